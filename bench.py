@@ -1,0 +1,255 @@
+"""Benchmark: batched flat-shell time stepping in DOF-steps/s on GB300.
+
+Default workload (N=1): 512 synthetic CFRP plates of U{40..80}^2 order-5
+elements (6.25 mm), damage zones, random actuators, carriers {50,75,100} kHz,
+FP32 stepping, advanced together (one fused kernel launch per time step,
+CUDA-graph chunks).  A bench "step" is one time step of the whole batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank advances its own 512 plates (seeded by rank;
+weak scaling, no data-path collective); the timed region is bracketed by a
+barrier and device synchronisation and rank 0 prints the max over ranks.
+``--impl reference`` times the reference's CPU algorithm (the FP64 oracle
+port, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+ALG_BYTES = {32: 16.0, 64: 32.0}   # algorithmic bytes per DOF-step (u_n, u_n-1, u_n+1, 1/M)
+METRIC = "DOF-steps/s (batched flat-shell SEM forward, 512 uneven plates)"
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        rank = int(os.environ["RANK"])
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        return rank, ws, local
+    return 0, 1, 0
+
+
+def barrier_sync(ws):
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.synchronize()
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(scenarios, run, steps, nthreads=0, budget_s=20.0):
+    """Oracle (FP64 port of the reference loop) on a bounded sample: the first
+    plates of the batch, `steps` time steps each, all host threads."""
+    from oracle.oracle import OracleProblem
+    done_dof_steps = 0
+    t_total = 0.0
+    used = 0
+    for sc in scenarios:
+        orc = OracleProblem(sc.mesh["nodes"], sc.mesh["coords"], sc.mat_table, sc.elem_mat, sc.elem_keep)
+        t0 = time.perf_counter()
+        orc.run(run.dt, run.nft, sc.signal, nn_first=run.nn_first, eta_xy=run.eta_xy, eta_z=run.eta_z,
+                force_dof=sc.force_dof, force_val=sc.force_val, out_dof=sc.out_dof, h=run.h,
+                nn_last=run.nn_first + steps - 1, nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+        done_dof_steps += 5 * sc.mesh["coords"].shape[0] * steps
+        used += 1
+        if t_total >= budget_s:
+            break
+    return done_dof_steps / t_total, used, t_total
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--plates", type=int, default=512)
+    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--graph", type=int, default=50)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank, ws, local = dist_init(args)
+    import __graft_entry__ as g
+    pkg = g.package()
+    W = pkg.workloads
+    scs, run = W.batch(n=args.plates, seed=1000 * rank)
+    ndof = W.dof_count(scs)
+    config = {"workload": f"batch of {args.plates} flat-shell plates, U{{40..80}}^2 order-5 elements (6.25 mm), "
+                          f"1-3 damage zones, random actuator, 5-cycle Hann {{50,75,100}} kHz, 0.4 ms",
+              "plates_per_gpu": args.plates, "dof_per_gpu": ndof, "dt_s": run.dt, "nft": run.nft,
+              "l2": "inputs larger than L2 (state %.2f GB per buffer)" % (ndof * args.precision / 8 / 1e9),
+              "parallelism": f"scenario shards x{ws}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(5, min(args.steps, 20))
+        vals = []
+        for _ in range(max(1, min(args.warmup, 1))):
+            cpu_reference(scs[:1], run, 3)
+        v, used, tt = cpu_reference(scs, run, steps, budget_s=20.0)
+        out = {"metric": METRIC, "value": v, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
+               "cpu_baseline": {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"first {used} plates x {steps} time steps, FP64 oracle restating "
+                                          "main_flat_shell.m:651-917, OpenMP over all host threads"},
+               "e2e": {"value": v, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    import torch
+    plan = pkg.Plan(scs, run, precision=args.precision, path=0, steps_per_graph=args.graph,
+                    tile_elems=args.tile, device=local)
+    plan.reset()
+    plan.set_signal()
+    nmax = run.nft - run.nn_first + 1
+    if args.warmup + args.steps > nmax:
+        raise SystemExit("warmup + steps exceed the run length")
+    plan.advance(args.warmup)
+    barrier_sync(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = plan.time_steps(args.steps)   # CUDA events on the plan's stream
+    torch.cuda.synchronize()
+    barrier_sync(ws)
+    ms = max_over_ranks(ms, ws)
+    sec = ms / 1e3
+    value = ndof * ws * args.steps / sec
+    per_launch_s = sec / args.steps
+    pk, pk_kind = peaks()
+    achieved = ALG_BYTES[args.precision] * ndof / per_launch_s / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": None,
+            "basis": f"{ALG_BYTES[args.precision]:.0f} B/DOF-step x {ndof} DOF per launch of "
+                     f"k_struct_step, CUDA events over {args.steps} launches; peak {pk_kind}"}
+    launches = args.steps * plan.info["launches_per_step"] + (args.steps // args.graph if args.graph else 1)
+
+    e2e = None
+    if not args.no_e2e:
+        # whole forward solve through the public API: H2D of the excitation,
+        # every time step, D2H of all sensor signals
+        t0 = time.perf_counter()
+        plan.forward()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        nsteps = run.nft - run.nn_first + 1
+        e2e_v = max_over_ranks(t1 - t0, ws)
+        nout = sum(len(s.out_dof) for s in scs)
+        e2e = {"value": ndof * ws * nsteps / e2e_v, "unit": "DOF-steps/s",
+               "h2d_bytes_per_step": 8 * len(scs), "d2h_bytes_per_step": 8 * nout,
+               "what": f"shm_forward of {nsteps} steps incl. signal upload and sensor download"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, used, tt = cpu_reference(scs, run, 10, budget_s=15.0)
+        cpu = {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"first {used} plates x 10 time steps ({tt:.1f} s), FP64 oracle, all host threads"}
+    plan.close()
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+               "config": config, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+               "gpu_launches": launches, "path": plan.info["path"], "tile": plan.info["tile"]}
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * shmsem.h -- C ABI of the GB300 spectral-element guided-wave engine.
+ *
+ * The engine replaces the explicit central-difference loop of ma-shm's
+ * MATLAB solvers (src/models/flat_shell/flat_shell_engine/main_flat_shell*.m,
+ * MAIN LOOP main_flat_shell.m:651-920) behind a plain C interface: plain
+ * pointers and sizes, MATLAB (column-major, 1-based) layouts at the boundary,
+ * integer status codes, no exceptions, no CUDA or torch types.  A MEX gateway
+ * (mexFunction) or a ctypes/cffi binding maps the solver's arguments onto
+ * these calls; see INTEGRATION.md.
+ *
+ * Ownership: the caller owns every host array it passes; the plan copies what
+ * it needs at creation and owns all device memory.  One plan is not
+ * re-entrant (one stream at a time); distinct plans may run concurrently.
+ */
+#ifndef SHMSEM_H
+#define SHMSEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SHM_OK = 0,
+  SHM_ERR_BAD_ARG = 1,     /* invalid argument (size, index, NULL pointer) */
+  SHM_ERR_CUDA = 2,        /* a CUDA call failed; shm_last_error() has the text */
+  SHM_ERR_DIVERGED = 3,    /* blow-up / non-finite guard (main_flat_shell.m:786-804) */
+  SHM_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  SHM_ERR_OOM = 5,         /* device allocation failed */
+  SHM_ERR_STATE = 6,       /* call out of order (e.g. outputs before a run) */
+  SHM_ERR_UNSUPPORTED = 7  /* option combination not built */
+} shm_status;
+
+typedef struct shm_plan shm_plan;
+
+/* Mesh of one scenario.  Replaces `load(meshfile)` (main_flat_shell.m:39):
+ * nodes(fen, npe), coords(nnode, 3), and optionally the 12-basket maps I_G,
+ * I_L produced by nodesMaps_Fiborek.m (when absent the library builds its
+ * own).  grid_nex/grid_ney > 0 declare a structured rectangular plate whose
+ * global nodes are numbered row by row (x fastest, see mesh.py); the library
+ * verifies that before it uses its structured fused kernel. */
+typedef struct {
+  int32_t fen;             /* number of elements */
+  int32_t npe;             /* nodes per element: 36 (order 5, 6x6 GLL) */
+  int32_t nnode;           /* number of nodes */
+  const int32_t *nodes;    /* [fen x npe] column-major, 1-based */
+  const double *coords;    /* [nnode x 3] column-major (x, y, z) */
+  int32_t basket_rows;     /* rows of I_G / I_L, 0 when not given */
+  const int32_t *I_G;      /* [basket_rows x 12] column-major, 1-based, 0 = empty */
+  const int32_t *I_L;      /* [basket_rows x 12] column-major, 1-based, 0 = empty */
+  int32_t grid_nex;        /* structured plate: elements along x (0 = unstructured) */
+  int32_t grid_ney;        /* structured plate: elements along y */
+} shm_mesh;
+
+/* Laminate of one scenario.  Replaces the outputs of composite_plate*.m
+ * (m11, I11, a11..d66), which the reference expands per local node; here one
+ * row per material plus a material index and a stiffness factor per element. */
+#define SHM_MAT_STRIDE 23
+typedef struct {
+  int32_t nmat;
+  const double *table;     /* [nmat x 23] row-major: a11 a12 a16 a22 a26 a66 a44 a45 a55
+                              b11 b12 b16 b22 b26 b66 d11 d12 d16 d22 d26 d66 m11 I11 */
+  const int32_t *elem_mat; /* [fen] 0-based material of each element, NULL = 0 */
+  const double *elem_keep; /* [fen] stiffness factor 1 - d_e of each element, NULL = 1 */
+} shm_material;
+
+/* Run parameters of one scenario (input*.m fields and the solver's derived
+ * vectors).  All scenarios of a batch must share dt, nft, nn_first, eta_*. */
+typedef struct {
+  double dt;               /* time step [s] (main_flat_shell.m:116) */
+  int32_t nft;             /* number of signal samples */
+  int32_t nn_first;        /* first loop index: 2 (main_flat_shell.m:651) or 1 (_multi_pzt_c.m:579) */
+  double eta_xy;           /* in-plane mass-proportional damping (etad_xy) */
+  double eta_z;            /* out-of-plane damping (etad_z) */
+  int32_t n_force;         /* nonzeros of the excitation vector Fi / Fa */
+  const int32_t *force_dof;  /* [n_force] 1-based global DOF, 5*(node-1)+{1..5} */
+  const double *force_val;   /* [n_force] value multiplying st(nn) */
+  int32_t n_out;           /* point outputs (main_flat_shell.m:752-764) */
+  const int32_t *out_dof;  /* [n_out] 1-based global DOF */
+  int32_t n_sens;          /* PZT sensors (main_flat_shell_multi_pzt_c.m:619-623) */
+  const int32_t *sens_ptr; /* [n_sens+1] CSR offsets into sens_el */
+  const int32_t *sens_el;  /* 0-based element numbers of each sensor */
+  double pzt_thickness;    /* sensor constants: Volt = t/g33*(e31*(..)+e32*(..)) */
+  double g33, e31, e32;
+  double h;                /* laminate thickness h (voltage lever arm, blow-up guard 10*h) */
+  int32_t frm_int;         /* frame interval in steps, 0 = no frames */
+  int32_t frame_dof;       /* 1..5: velocity component stored in frames (5 = w) */
+} shm_run;
+
+typedef struct {
+  int32_t precision;       /* 64 or 32 (state and element arithmetic) */
+  int32_t path;            /* 0 auto, 1 general (element + node kernels), 2 structured fused */
+  int32_t steps_per_graph; /* CUDA-graph chunk length, 0 = plain launches */
+  int32_t tile_elems;      /* structured path: elements per warp line (16/32), 0 = autotune */
+  int32_t device;          /* CUDA device ordinal */
+} shm_options;
+
+/* Creates a plan for `nscen` scenarios advanced together (one launch per
+ * kernel per step covers all of them).  Replaces the set-up part of
+ * main_flat_shell*.m (:35-650): geometry, mass, maps, device upload. */
+shm_status shm_plan_create(int32_t nscen, const shm_mesh *meshes, const shm_material *mats,
+                           const shm_run *runs, const shm_options *opt, shm_plan **out);
+shm_status shm_plan_destroy(shm_plan *plan);
+const char *shm_last_error(const shm_plan *plan);
+
+/* Whole forward solve, the MAIN LOOP (main_flat_shell.m:651-917).
+ *   st      [nscen][nft]            excitation samples st(nn) (Hanning_signal.m)
+ *   displ   [nscen][n_out x nft]    column-major per scenario (displ, :926)
+ *   voltage [nscen][nft x n_sens]   column-major per scenario (voltage, :925)
+ *   frames  [nscen][nframes x nnode] velocity frames, frame-major (V?_frame<c>)
+ * Any output pointer may be NULL.  `stream` is a cudaStream_t or NULL. */
+shm_status shm_forward(shm_plan *plan, const double *st, double *displ, double *voltage,
+                       double *frames, void *stream);
+
+/* Fine-grained stepping used by forward/adjoint drivers and benchmarks. */
+shm_status shm_reset(shm_plan *plan);                        /* zero state, nn = nn_first */
+shm_status shm_set_signal(shm_plan *plan, const double *st, void *stream);
+shm_status shm_advance(shm_plan *plan, int32_t nsteps, void *stream);
+shm_status shm_read_outputs(shm_plan *plan, double *displ, double *voltage, double *frames,
+                            void *stream);
+/* Device time of `nsteps` steps (CUDA events on the plan's stream). */
+shm_status shm_time_steps(shm_plan *plan, int32_t nsteps, float *ms);
+
+/* State in the reference's DOF layout: [total_nodes x 5] interleaved
+ * (u, phi_x, v, phi_y, w per node), scenarios concatenated. */
+shm_status shm_get_state(shm_plan *plan, double *U, double *uold);
+shm_status shm_set_state(shm_plan *plan, const double *U, const double *uold, int32_t nn);
+
+/* Assembled internal force K*U for a given state (same layout), no update. */
+shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
+
+/* Plan facts: [0] total nodes, [1] total elements, [2] total DOF, [3] path
+ * used (1 general, 2 structured), [4] precision, [5] frames per scenario,
+ * [6] kernel launches per step, [7] tile elements (structured). */
+shm_status shm_plan_info(const shm_plan *plan, int64_t *info8);
+
+/* Diagonal mass vector of the plan (reference mg before scaling, :493-501),
+ * [total_nodes x 5] interleaved. */
+shm_status shm_mass(shm_plan *plan, double *mg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHMSEM_H */

@@ -1,0 +1,1378 @@
+// shmsem.cu -- C ABI, plan set-up and the general (unstructured) flat-shell
+// step of the GB300 spectral-element engine.
+//
+// One time step of the reference MAIN LOOP (main_flat_shell.m:651-750) is two
+// kernels on the general path:
+//   k_elem_general  gather (:655-659) + derivatives (:661-671) + resultants
+//                   (:674-681) + transposed operators (:683-689) + PZT voltage
+//                   partials (:690-692); element-local forces go to a scratch
+//                   array laid out like the reference's F2 (:716-721);
+//   k_node_general  deterministic assembly (the 12-basket scatter :724-726,
+//                   summed per node in basket order) + the central-difference
+//                   update (:742-750) + frames / blow-up guard (:767-804).
+// The structured fused path (one kernel per step, no scratch) is in
+// shell_structured.cuh.  Both are instantiated for double and float.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "shmsem.h"
+#include "shell_element.cuh"
+
+using namespace shm;
+
+// ---------------------------------------------------------------------------
+// device kernels: general path
+// ---------------------------------------------------------------------------
+
+template <typename T> struct GenArgs {
+  // sizes
+  int64_t fen_pad, nnode_pad, plane;  // plane: length of one F2 field plane
+  int nnode, fen, nn_first, nft;
+  // state (two SoA buffers [5][nnode_pad]) and scratch [5][plane]
+  T* UA;
+  T* UB;
+  T* F2;
+  // mesh
+  const int* __restrict__ conn;   // [36][fen_pad], 0-based global nodes
+  const T* __restrict__ geo;      // [5][36][fen_pad]
+  const int* __restrict__ emat;   // [fen_pad]
+  const T* __restrict__ ekeep;    // [fen_pad]
+  const T* __restrict__ mat;      // [nmat][24]
+  const int* __restrict__ row_ptr;
+  const int* __restrict__ slots;
+  const T* __restrict__ minv;     // [2][nnode_pad]: 1/M translational, rotational
+  T k1[5], k2[5];                 // update coefficients per field
+  // excitation: force slots appended after 36*fen_pad in every plane
+  int nforce;
+  const int* __restrict__ fq_field;
+  const int* __restrict__ fq_scen;
+  const double* __restrict__ fq_val;
+  const double* __restrict__ st;  // [nscen][nft]
+  // point outputs
+  int nout;
+  const int* __restrict__ out_node;
+  const int* __restrict__ out_field;
+  double* displ;                  // [nout][nft]
+  // PZT sensor partial sums
+  const int* __restrict__ esens;  // [fen_pad] slot or -1
+  double* vsum;                   // [nslot][nft]
+  SensorConst<T> sc;
+  // frames
+  int frm_int, frame_field, nframes;
+  T* frames;                      // [nframes][nnode_pad]
+  T a1;
+  T blowup;                       // 10*h
+  int* flag;
+  const int* d_base;
+};
+
+template <typename T>
+__device__ __forceinline__ void block0_duties(const GenArgs<T>& a, const T* cur, int nn) {
+  // excitation samples into the force slots (F2 holds +K*u, so store -f*st)
+  const int64_t p36 = (int64_t)NPE * a.fen_pad;
+  for (int q = threadIdx.x; q < a.nforce; q += blockDim.x) {
+    const double s = a.st[(int64_t)a.fq_scen[q] * a.nft + (nn - 1)];
+    const T val = (T)(-a.fq_val[q] * s);
+#pragma unroll
+    for (int f = 0; f < 5; ++f) a.F2[f * a.plane + p36 + q] = (f == a.fq_field[q]) ? val : T(0);
+  }
+  // displ(nn,:) = U(outputs): state at the start of the step
+  for (int q = threadIdx.x; q < a.nout; q += blockDim.x)
+    a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
+}
+
+template <typename T, bool kSensor>
+__global__ void __launch_bounds__(CTA_THREADS) k_elem_general(GenArgs<T> a, int kstep) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int nn = *a.d_base + kstep;
+  const T* __restrict__ cur = ((nn - a.nn_first) & 1) ? a.UB : a.UA;
+  if (blockIdx.x == 0) block0_duties(a, cur, nn);
+
+  const int j = threadIdx.x >> 5;   // line (row in phase A/C, column in B)
+  const int le = threadIdx.x & 31;  // element within the CTA
+  const int e = blockIdx.x * CTA_ELEMS + le;
+  T* xs = sm + le * ELEM_STRIDE;
+  T* ys = sm + (CTA_ELEMS + le) * ELEM_STRIDE;
+  T* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;  // [6][32] sensor partials
+
+  // phase A: gather row j of element e (UX=U(Iu) ... :655-659)
+  {
+    T u[5][NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int node = a.conn[(int64_t)(j * NP + i) * a.fen_pad + e];
+#pragma unroll
+      for (int f = 0; f < 5; ++f) u[f][i] = cur[f * a.nnode_pad + node];
+    }
+    row_deriv_store(u, xs, ys, j);
+  }
+  __syncthreads();
+  // phase B: column i = j
+  {
+    const int i = j;
+    T v[5][NP];
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+#pragma unroll
+      for (int k = 0; k < NP; ++k) v[f][k] = xs[f * NPE + i * NP + k];
+    const Lam<T> L = load_lam(a.mat + (int64_t)a.emat[e] * MAT_STRIDE_DEV, a.ekeep[e]);
+    GeoGeneral<T> geo{a.geo, a.fen_pad, e};
+    T Fe[5][NP];
+    const T vp = shell_column<T, GeoGeneral<T>, kSensor>(v, ys, xs, i, L, geo, Fe, a.sc);
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+#pragma unroll
+      for (int m = 0; m < NP; ++m) ys[f * NPE + i * NP + m] = Fe[f][m];
+    if (kSensor) vred[i * CTA_ELEMS + le] = vp;
+  }
+  __syncthreads();
+  // phase C + write element-local forces F2[f][c][e], c = j*6 + i
+  {
+    T out[5][NP];
+    row_transpose_apply(xs, ys, j, out);
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+#pragma unroll
+      for (int i = 0; i < NP; ++i) a.F2[f * a.plane + (int64_t)(j * NP + i) * a.fen_pad + e] = out[f][i];
+  }
+  if (kSensor && j == 0 && e < a.fen) {
+    const int slot = a.esens[e];
+    if (slot >= 0) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < NP; ++i) s += (double)vred[i * CTA_ELEMS + le];
+      a.vsum[(int64_t)slot * a.nft + (nn - 1)] = s;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
+  const int nn = *a.d_base + kstep;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.nnode) return;
+  const bool odd = ((nn - a.nn_first) & 1);
+  const T* __restrict__ cur = odd ? a.UB : a.UA;
+  T* prev = odd ? a.UA : a.UB;
+  T F[5] = {T(0), T(0), T(0), T(0), T(0)};
+  const int s0 = a.row_ptr[g], s1 = a.row_ptr[g + 1];
+  for (int s = s0; s < s1; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
+  const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
+  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  bool bad = false;
+#pragma unroll
+  for (int f = 0; f < 5; ++f) {
+    const T u = cur[f * a.nnode_pad + g];
+    const T uo = prev[f * a.nnode_pad + g];
+    const T im = (f == 1 || f == 3) ? mr : mt;
+    // unew = mg0.*(-F + mg2.*U - mg.*uold + a1*cg.*uold) rewritten as
+    // u + k1*(u-uold) - k2*(F/M); F already contains -Fa*st(nn)
+    const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
+    prev[f * a.nnode_pad + g] = un;
+    if (frame) {
+      if (f == a.frame_field) {
+        const int fc = nn / a.frm_int - 1;
+        if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + g] = a.a1 * (un - uo);
+      }
+      if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
+    }
+  }
+  if (bad) atomicOr(a.flag, 1);
+}
+
+// assembled K*u only (no update), into out[5][nnode_pad]
+template <typename T>
+__global__ void k_assemble_only(GenArgs<T> a, T* out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.nnode) return;
+  T F[5] = {T(0), T(0), T(0), T(0), T(0)};
+  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
+#pragma unroll
+  for (int f = 0; f < 5; ++f) out[f * a.nnode_pad + g] = F[f];
+}
+
+__global__ void k_advance(int* d_base, int n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *d_base += n;
+}
+
+// voltage(nn,k) = mean over the sensor's local nodes (FP64)
+__global__ void k_voltage(const double* vsum, const int* sptr, double* volt, int nsens, int nft) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsens * nft) return;
+  const int k = t / nft, n = t % nft;
+  double s = 0.0;
+  for (int q = sptr[k]; q < sptr[k + 1]; ++q) s += vsum[(int64_t)q * nft + n];
+  const int cnt = (sptr[k + 1] - sptr[k]) * NPE;
+  volt[(int64_t)k * nft + n] = cnt ? s / cnt : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// structured fused path (declared here, defined in shell_structured.cuh)
+// ---------------------------------------------------------------------------
+#include "shell_structured.cuh"
+
+struct StructPlan {
+  int tile = 32, H = 16, ntask = 0, grid = 0;
+  PlateDesc* plates = nullptr;
+  TaskDesc* tasks = nullptr;
+  int* emat_g = nullptr;
+  void* ekeep_g = nullptr;
+  int* esens_g = nullptr;
+  int *f_xl = nullptr, *f_iy = nullptr, *f_field = nullptr;
+  double* f_val = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct shm_plan {
+  std::string err;
+  int prec = 64, path = 1, device = 0, steps_per_graph = 0, tile = 0;
+  cudaStream_t stream = nullptr;
+  int nscen = 0;
+  int nft = 0, nn_first = 2, nn = 2;
+  double dt = 0, a0 = 0, a1 = 0;
+  int64_t nnode = 0, fen = 0, fen_pad = 0, nnode_pad = 0, plane = 0;
+  std::vector<int64_t> node_off, elem_off;
+  std::vector<int> out_off, sens_off, nout_s, nsens_s;
+  int nout = 0, nsens = 0, nslot = 0, nforce = 0;
+  int frm_int = 0, frame_field = 4, nframes = 0;
+  std::vector<double> mass;  // [nnode][5] host copy (interleaved)
+  // device memory
+  std::vector<void*> allocs;
+  void *UA = nullptr, *UB = nullptr, *F2 = nullptr, *geo = nullptr, *ekeep = nullptr, *mat = nullptr,
+       *minv = nullptr, *frames = nullptr;
+  int *conn = nullptr, *emat = nullptr, *row_ptr = nullptr, *slots = nullptr;
+  int *fq_field = nullptr, *fq_scen = nullptr, *out_node = nullptr, *out_field = nullptr;
+  int *esens = nullptr, *sptr = nullptr, *flag = nullptr, *d_base = nullptr;
+  double *fq_val = nullptr, *st = nullptr, *displ = nullptr, *vsum = nullptr, *volt = nullptr;
+  double k1[5], k2[5];
+  double blowup = 0;
+  double sc_k0 = 0, sc_e31 = 0, sc_e32 = 0, sc_hh = 0;
+  // structured path
+  StructPlan sp;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  int gsteps = 0;
+  bool ran = false;
+};
+
+#define CKP(plan, call)                                                               \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess) {                                                          \
+      (plan)->err = std::string(#call) + ": " + cudaGetErrorString(e_);               \
+      return (e_ == cudaErrorMemoryAllocation) ? SHM_ERR_OOM : SHM_ERR_CUDA;          \
+    }                                                                                 \
+  } while (0)
+
+static shm_status bad(shm_plan* p, const std::string& m) {
+  if (p) p->err = m;
+  return SHM_ERR_BAD_ARG;
+}
+
+template <typename X>
+static shm_status dalloc(shm_plan* p, X** out, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(X);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    p->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return SHM_ERR_OOM;
+  }
+  cudaMemset(q, 0, bytes);
+  p->allocs.push_back(q);
+  *out = reinterpret_cast<X*>(q);
+  return SHM_OK;
+}
+
+template <typename X>
+static shm_status upload(shm_plan* p, X** out, const std::vector<X>& v) {
+  shm_status s = dalloc(p, out, v.size());
+  if (s != SHM_OK) return s;
+  if (!v.empty()) CKP(p, cudaMemcpy(*out, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
+  return SHM_OK;
+}
+
+// GLL nodes/weights (Newton on P'_{n-1} from Chebyshev-Lobatto guesses) and
+// the Lagrange derivative matrix by barycentric weights.
+static void gll_setup(int n, std::vector<double>& x, std::vector<double>& w, std::vector<double>& D) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const int N = n - 1;
+  auto legendre = [N](double t, double& p, double& dp, double& d2p) {
+    double p0 = 1.0, p1 = t;
+    if (N == 0) { p = 1; dp = 0; d2p = 0; return; }
+    for (int k = 2; k <= N; ++k) {
+      double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    p = p1;
+    // P' and P'' from the Legendre ODE where |t| < 1
+    dp = N * (t * p1 - p0) / (t * t - 1.0);
+    d2p = (2.0 * t * dp - N * (N + 1.0) * p) / (1.0 - t * t);
+  };
+  x[0] = -1.0;
+  x[N] = 1.0;
+  for (int k = 1; k < N; ++k) {
+    double t = -std::cos(M_PI * k / N);
+    for (int it = 0; it < 100; ++it) {
+      double p, dp, d2p;
+      legendre(t, p, dp, d2p);
+      double dt = dp / d2p;
+      t -= dt;
+      if (std::fabs(dt) < 1e-16) break;
+    }
+    x[k] = t;
+  }
+  for (int k = 0; k <= N / 2; ++k) {  // exact symmetry
+    double s = 0.5 * (x[N - k] - x[k]);
+    x[k] = -s;
+    x[N - k] = s;
+  }
+  if (n % 2 == 1) x[N / 2] = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double p0 = 1.0, p1 = x[k];
+    for (int m = 2; m <= N; ++m) {
+      double p2 = ((2.0 * m - 1.0) * x[k] * p1 - (m - 1.0) * p0) / m;
+      p0 = p1;
+      p1 = p2;
+    }
+    w[k] = 2.0 / (N * (N + 1.0) * p1 * p1);
+  }
+  std::vector<double> lam(n, 1.0);
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < n; ++k)
+      if (k != j) lam[j] /= (x[j] - x[k]);
+  D.assign(n * n, 0.0);
+  for (int r = 0; r < n; ++r) {
+    double diag = 0.0;
+    for (int c = 0; c < n; ++c)
+      if (c != r) {
+        D[r * n + c] = (lam[c] / lam[r]) / (x[r] - x[c]);
+        diag -= D[r * n + c];
+      }
+    D[r * n + r] = diag;
+  }
+  // the reference zeroes |entries| < 1e-12 of its derivative operators
+  // (shape2D_prim.m:52,54): interior diagonal entries are exactly 0
+  for (double& v : D)
+    if (std::fabs(v) < 1e-12) v = 0.0;
+}
+
+// 12-basket maps (nodesMaps_Fiborek.m): every element copy of a node goes to
+// the least-filled basket, ties to the lowest basket number.  Only the
+// per-node summation order is taken from it.
+static void build_baskets(int fen, int npe, int nnode, const int32_t* nodes_cm,
+                          std::vector<int>& IG, std::vector<int>& IL, int& rows) {
+  std::vector<int> psi(nnode + 1, 0);
+  std::vector<int> start(nnode + 2, 0);
+  for (int e = 0; e < fen; ++e)
+    for (int c = 0; c < npe; ++c) psi[nodes_cm[(int64_t)c * fen + e]]++;
+  for (int k = 1; k <= nnode; ++k) start[k + 1] = start[k] + psi[k];
+  std::vector<int> fill(nnode + 2, 0), copyE(start[nnode + 1]), copyL(start[nnode + 1]);
+  for (int e = 0; e < fen; ++e)
+    for (int c = 0; c < npe; ++c) {
+      int k = nodes_cm[(int64_t)c * fen + e];
+      int pos = start[k] + fill[k]++;
+      copyE[pos] = e + 1;
+      copyL[pos] = c + 1;
+    }
+  rows = (npe * fen + 11) / 12;
+  int maxrows = rows + 12;
+  IG.assign((size_t)maxrows * 12, 0);
+  IL.assign((size_t)maxrows * 12, 0);
+  int H[12] = {0};
+  for (int k = 1; k <= nnode; ++k) {
+    int S[12];
+    for (int b = 0; b < 12; ++b) S[b] = b;
+    std::stable_sort(S, S + 12, [&](int a, int b) { return H[a] < H[b]; });
+    for (int i = 0; i < psi[k] && i < 12; ++i) {
+      int b = S[i];
+      H[b]++;
+      int pos = start[k] + i;
+      IG[(size_t)b * maxrows + H[b] - 1] = k;
+      IL[(size_t)b * maxrows + H[b] - 1] = (copyE[pos] - 1) * npe + copyL[pos];
+    }
+  }
+  int mr = 0;
+  for (int b = 0; b < 12; ++b) mr = std::max(mr, H[b]);
+  // compact to column-major [mr x 12]
+  std::vector<int> G2((size_t)mr * 12), L2((size_t)mr * 12);
+  for (int b = 0; b < 12; ++b)
+    for (int r = 0; r < mr; ++r) {
+      G2[(size_t)b * mr + r] = IG[(size_t)b * maxrows + r];
+      L2[(size_t)b * mr + r] = IL[(size_t)b * maxrows + r];
+    }
+  IG.swap(G2);
+  IL.swap(L2);
+  rows = mr;
+}
+
+template <typename T> static void fill_sc(shm_plan* p, SensorConst<T>& sc) {
+  sc.k0 = (T)p->sc_k0;
+  sc.e31 = (T)p->sc_e31;
+  sc.e32 = (T)p->sc_e32;
+  sc.hh = (T)p->sc_hh;
+}
+
+template <typename T> static GenArgs<T> make_args(shm_plan* p) {
+  GenArgs<T> a;
+  a.fen_pad = p->fen_pad;
+  a.nnode_pad = p->nnode_pad;
+  a.plane = p->plane;
+  a.nnode = (int)p->nnode;
+  a.fen = (int)p->fen;
+  a.nn_first = p->nn_first;
+  a.nft = p->nft;
+  a.UA = (T*)p->UA;
+  a.UB = (T*)p->UB;
+  a.F2 = (T*)p->F2;
+  a.conn = p->conn;
+  a.geo = (const T*)p->geo;
+  a.emat = p->emat;
+  a.ekeep = (const T*)p->ekeep;
+  a.mat = (const T*)p->mat;
+  a.row_ptr = p->row_ptr;
+  a.slots = p->slots;
+  a.minv = (const T*)p->minv;
+  for (int f = 0; f < 5; ++f) {
+    a.k1[f] = (T)p->k1[f];
+    a.k2[f] = (T)p->k2[f];
+  }
+  a.nforce = p->nforce;
+  a.fq_field = p->fq_field;
+  a.fq_scen = p->fq_scen;
+  a.fq_val = p->fq_val;
+  a.st = p->st;
+  a.nout = p->nout;
+  a.out_node = p->out_node;
+  a.out_field = p->out_field;
+  a.displ = p->displ;
+  a.esens = p->esens;
+  a.vsum = p->vsum;
+  fill_sc(p, a.sc);
+  a.frm_int = p->frm_int;
+  a.frame_field = p->frame_field;
+  a.nframes = p->nframes;
+  a.frames = (T*)p->frames;
+  a.a1 = (T)p->a1;
+  a.blowup = (T)p->blowup;
+  a.flag = p->flag;
+  a.d_base = p->d_base;
+  return a;
+}
+
+static size_t elem_smem_bytes(int prec) {
+  const size_t ts = prec == 64 ? 8 : 4;
+  return ts * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS);
+}
+
+template <typename T>
+static cudaError_t launch_general_step(shm_plan* p, int kstep, cudaStream_t s) {
+  GenArgs<T> a = make_args<T>(p);
+  const int nblk = (int)(p->fen_pad / CTA_ELEMS);
+  const size_t sm = elem_smem_bytes(sizeof(T) == 8 ? 64 : 32);
+  if (p->nslot > 0)
+    k_elem_general<T, true><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
+  else
+    k_elem_general<T, false><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
+  k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kstep);
+  return cudaGetLastError();
+}
+
+template <typename T> static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s);
+
+static cudaError_t launch_step(shm_plan* p, int kstep, cudaStream_t s) {
+  if (p->path == 2) {
+    return p->prec == 64 ? launch_struct_step<double>(p, kstep, s) : launch_struct_step<float>(p, kstep, s);
+  }
+  return p->prec == 64 ? launch_general_step<double>(p, kstep, s) : launch_general_step<float>(p, kstep, s);
+}
+
+static shm_status set_func_attrs(shm_plan* p) {
+  const int sm64 = (int)elem_smem_bytes(64), sm32 = (int)elem_smem_bytes(32);
+  CKP(p, cudaFuncSetAttribute(k_elem_general<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+  CKP(p, cudaFuncSetAttribute(k_struct_step<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_smem_bytes<double, 32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_smem_bytes<double, 16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_smem_bytes<float, 32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_smem_bytes<float, 16>()));
+  return SHM_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// structured path: plan build and launch
+// ---------------------------------------------------------------------------
+
+// lanes doing useful work for strips of EW lanes (EW-1 owned elements each)
+static double lane_utilisation(const shm_mesh* meshes, int nscen, int EW) {
+  double used = 0, total = 0;
+  for (int s = 0; s < nscen; ++s) {
+    const int nex = meshes[s].grid_nex, ney = meshes[s].grid_ney, NX = 5 * nex + 1;
+    const int own = 5 * (EW - 1);
+    const int ns = (NX + own - 1) / own;
+    for (int k = 0; k < ns; ++k) {
+      int valid = 0;
+      for (int q = 0; q < EW; ++q) {
+        const int ex = k * (EW - 1) - 1 + q;
+        valid += (ex >= 0 && ex < nex);
+      }
+      used += (double)valid * ney;
+      total += (double)EW * ney;
+    }
+  }
+  return total > 0 ? used / total : 0;
+}
+
+static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, const shm_material* mats,
+                               const shm_run* runs, int tile_elems, const std::vector<double>& gw,
+                               const std::vector<double>& geo, const std::vector<int>& emat,
+                               const std::vector<double>& ekeep, const std::vector<int>& esens,
+                               const std::vector<int>& fq_field, const std::vector<double>& fq_val,
+                               std::string& why) {
+  (void)mats;
+  (void)fq_field;
+  (void)fq_val;
+  StructPlan& sp = p->sp;
+  const int64_t FP = p->fen_pad;
+  std::vector<PlateDesc> plates(nscen);
+  int64_t egrid = 0;
+  std::vector<int> emat_g(p->fen), esens_g(p->fen, -1);
+  std::vector<double> ekeep_g(p->fen, 1.0);
+  for (int s = 0; s < nscen; ++s) {
+    const shm_mesh& m = meshes[s];
+    const int nex = m.grid_nex, ney = m.grid_ney;
+    if (nex < 1 || ney < 1) { why = "mesh is not declared structured"; return SHM_ERR_UNSUPPORTED; }
+    const int NX = 5 * nex + 1, NY = 5 * ney + 1;
+    if ((int64_t)m.nnode != (int64_t)NX * NY || m.fen != nex * ney) { why = "grid sizes do not match the mesh"; return SHM_ERR_UNSUPPORTED; }
+    std::vector<char> seen((size_t)nex * ney, 0);
+    const int64_t e0 = p->elem_off[s];
+    double sx = 0, sy = 0, a4 = 0;
+    for (int e = 0; e < m.fen; ++e) {
+      const int b0 = m.nodes[e] - 1;  // c = 0
+      const int ix0 = b0 % NX, iy0 = b0 / NX;
+      if (ix0 % 5 || iy0 % 5 || ix0 / 5 >= nex || iy0 / 5 >= ney) { why = "element origin off the grid"; return SHM_ERR_UNSUPPORTED; }
+      for (int k = 0; k < NP; ++k)
+        for (int i = 0; i < NP; ++i)
+          if (m.nodes[(int64_t)(k * NP + i) * m.fen + e] - 1 != (iy0 + k) * NX + ix0 + i) {
+            why = "connectivity is not the row-major grid numbering";
+            return SHM_ERR_UNSUPPORTED;
+          }
+      const int ex = ix0 / 5, ey = iy0 / 5;
+      if (seen[(size_t)ey * nex + ex]++) { why = "duplicate element"; return SHM_ERR_UNSUPPORTED; }
+      const int64_t ge = e0 + e;
+      for (int c = 0; c < NPE; ++c) {
+        const int64_t base = (int64_t)c * FP + ge;
+        const double i11 = geo[0 * NPE * FP + base], i12 = geo[1 * NPE * FP + base];
+        const double i21 = geo[2 * NPE * FP + base], i22 = geo[3 * NPE * FP + base];
+        const double W = geo[4 * NPE * FP + base] / (gw[c % NP] * gw[c / NP]);
+        if (e == 0 && c == 0) { sx = i11; sy = i22; a4 = W; }
+        const double tol = 1e-9;
+        if (std::fabs(i12) > 1e-12 * std::fabs(i11) || std::fabs(i21) > 1e-12 * std::fabs(i22) ||
+            std::fabs(i11 - sx) > tol * std::fabs(sx) || std::fabs(i22 - sy) > tol * std::fabs(sy) ||
+            std::fabs(W - a4) > tol * std::fabs(a4)) {
+          why = "elements are not equal axis-aligned rectangles";
+          return SHM_ERR_UNSUPPORTED;
+        }
+      }
+      emat_g[egrid + (int64_t)ey * nex + ex] = emat[ge];
+      ekeep_g[egrid + (int64_t)ey * nex + ex] = ekeep[ge];
+      esens_g[egrid + (int64_t)ey * nex + ex] = esens[ge];
+    }
+    plates[s] = PlateDesc{nex, ney, NX, s, (long long)p->node_off[s], (long long)egrid, sx, sy, a4};
+    egrid += (int64_t)nex * ney;
+  }
+  // tile (elements per warp line) and rows per block
+  int EW = tile_elems;
+  if (EW != 16 && EW != 32) EW = lane_utilisation(meshes, nscen, 32) >= 0.9 * lane_utilisation(meshes, nscen, 16) ? 32 : 16;
+  const int own = 5 * (EW - 1);
+  int H = 16;
+  sp.tile = EW;
+  sp.H = H;
+  struct TaskTmp { TaskDesc t; std::vector<int> fxl, fiy, ffield; std::vector<double> fval; };
+  std::vector<TaskTmp> tasks;
+  std::vector<std::vector<int>> task_index(nscen);
+  for (int s = 0; s < nscen; ++s) {
+    const PlateDesc& pl = plates[s];
+    const int ns = (pl.NX + own - 1) / own, nb = (pl.ney + H - 1) / H;
+    task_index[s].assign((size_t)ns * nb, -1);
+    for (int b = 0; b < nb; ++b)
+      for (int k = 0; k < ns; ++k) {
+        TaskTmp t;
+        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};
+        const int last = std::min(H * (b + 1), pl.ney);
+        t.t.nrows = b == 0 ? last : last - (H * b - 1);
+        task_index[s][(size_t)b * ns + k] = (int)tasks.size();
+        tasks.push_back(std::move(t));
+      }
+    for (int q = 0; q < runs[s].n_force; ++q) {
+      const int d = runs[s].force_dof[q];
+      const int node = (d - 1) / 5, field = (d - 1) % 5;
+      const int ix = node % pl.NX, iy = node / pl.NX;
+      const int k = ix / own;
+      const int b = std::min(iy / (5 * H), nb - 1);
+      TaskTmp& t = tasks[task_index[s][(size_t)b * ns + k]];
+      t.fxl.push_back(ix - 5 * (k * (EW - 1) - 1));
+      t.fiy.push_back(iy);
+      t.ffield.push_back(field);
+      t.fval.push_back(runs[s].force_val[q]);
+    }
+  }
+  // longest tasks first so that lane groups of a CTA stay in step
+  std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
+  std::vector<TaskDesc> td;
+  std::vector<int> fxl, fiy, ffield;
+  std::vector<double> fval;
+  for (TaskTmp& t : tasks) {
+    t.t.f0 = (int)fxl.size();
+    t.t.fn = (int)t.fxl.size();
+    fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
+    fiy.insert(fiy.end(), t.fiy.begin(), t.fiy.end());
+    ffield.insert(ffield.end(), t.ffield.begin(), t.ffield.end());
+    fval.insert(fval.end(), t.fval.begin(), t.fval.end());
+    td.push_back(t.t);
+  }
+  sp.ntask = (int)td.size();
+  shm_status st;
+  {
+    PlateDesc* dp = nullptr;
+    TaskDesc* dt = nullptr;
+    if ((st = upload(p, &dp, plates)) != SHM_OK) return st;
+    if ((st = upload(p, &dt, td)) != SHM_OK) return st;
+    sp.plates = dp;
+    sp.tasks = dt;
+  }
+  if ((st = upload(p, &sp.emat_g, emat_g)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.esens_g, esens_g)) != SHM_OK) return st;
+  if (p->prec == 64) {
+    double* k = nullptr;
+    if ((st = upload(p, &k, ekeep_g)) != SHM_OK) return st;
+    sp.ekeep_g = k;
+  } else {
+    std::vector<float> k32(ekeep_g.begin(), ekeep_g.end());
+    float* k = nullptr;
+    if ((st = upload(p, &k, k32)) != SHM_OK) return st;
+    sp.ekeep_g = k;
+  }
+  if ((st = upload(p, &sp.f_xl, fxl)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_iy, fiy)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_field, ffield)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_val, fval)) != SHM_OK) return st;
+  const int G = 32 / EW;
+  sp.grid = (sp.ntask + G - 1) / G;
+  return SHM_OK;
+}
+
+template <typename T>
+static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
+  StructPlan& sp = p->sp;
+  StructArgs<T> a;
+  a.plates = sp.plates;
+  a.tasks = sp.tasks;
+  a.ntask = sp.ntask;
+  a.H = sp.H;
+  a.nn_first = p->nn_first;
+  a.nft = p->nft;
+  a.nnode_pad = p->nnode_pad;
+  a.UA = (T*)p->UA;
+  a.UB = (T*)p->UB;
+  a.minv = (const T*)p->minv;
+  for (int f = 0; f < 5; ++f) {
+    a.k1[f] = (T)p->k1[f];
+    a.k2[f] = (T)p->k2[f];
+  }
+  a.mat = (const T*)p->mat;
+  a.emat_g = sp.emat_g;
+  a.ekeep_g = (const T*)sp.ekeep_g;
+  a.esens_g = sp.esens_g;
+  a.f_xl = sp.f_xl;
+  a.f_iy = sp.f_iy;
+  a.f_field = sp.f_field;
+  a.f_val = sp.f_val;
+  a.st = p->st;
+  a.nout = p->nout;
+  a.out_node = p->out_node;
+  a.out_field = p->out_field;
+  a.displ = p->displ;
+  a.vsum = p->vsum;
+  fill_sc(p, a.sc);
+  a.frm_int = p->frm_int;
+  a.frame_field = p->frame_field;
+  a.nframes = p->nframes;
+  a.frames = (T*)p->frames;
+  a.a1 = (T)p->a1;
+  a.blowup = (T)p->blowup;
+  a.flag = p->flag;
+  a.d_base = p->d_base;
+  if (sp.tile == 32)
+    k_struct_step<T, 32><<<sp.grid, CTA_THREADS, struct_smem_bytes<T, 32>(), s>>>(a, kstep);
+  else
+    k_struct_step<T, 16><<<sp.grid, CTA_THREADS, struct_smem_bytes<T, 16>(), s>>>(a, kstep);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// plan creation
+// ---------------------------------------------------------------------------
+
+template <typename T>
+static shm_status build_device(shm_plan* p, const std::vector<int>& conn, const std::vector<double>& geo,
+                               const std::vector<int>& emat, const std::vector<double>& ekeep,
+                               const std::vector<double>& mat, const std::vector<double>& minv) {
+  shm_status s;
+  auto conv = [](const std::vector<double>& v) {
+    std::vector<T> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) o[i] = (T)v[i];
+    return o;
+  };
+  T *g = nullptr, *k = nullptr, *m = nullptr, *mi = nullptr, *ua = nullptr, *ub = nullptr, *f2 = nullptr,
+    *fr = nullptr;
+  if ((s = upload(p, &p->conn, conn)) != SHM_OK) return s;
+  if ((s = upload(p, &g, conv(geo))) != SHM_OK) return s;
+  if ((s = upload(p, &p->emat, emat)) != SHM_OK) return s;
+  if ((s = upload(p, &k, conv(ekeep))) != SHM_OK) return s;
+  if ((s = upload(p, &m, conv(mat))) != SHM_OK) return s;
+  if ((s = upload(p, &mi, conv(minv))) != SHM_OK) return s;
+  if ((s = dalloc(p, &ua, (size_t)5 * p->nnode_pad)) != SHM_OK) return s;
+  if ((s = dalloc(p, &ub, (size_t)5 * p->nnode_pad)) != SHM_OK) return s;
+  if ((s = dalloc(p, &f2, (size_t)5 * p->plane)) != SHM_OK) return s;
+  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nnode_pad)) != SHM_OK) return s;
+  p->geo = g;
+  p->ekeep = k;
+  p->mat = m;
+  p->minv = mi;
+  p->UA = ua;
+  p->UB = ub;
+  p->F2 = f2;
+  p->frames = fr;
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, const shm_material* mats,
+                                      const shm_run* runs, const shm_options* opt, shm_plan** out) {
+  if (!out) return SHM_ERR_BAD_ARG;
+  *out = nullptr;
+  if (nscen < 1 || !meshes || !mats || !runs) return SHM_ERR_BAD_ARG;
+  shm_plan* p = new shm_plan();
+  *out = p;
+  shm_options o{};
+  o.precision = 64;
+  if (opt) o = *opt;
+  if (o.precision != 64 && o.precision != 32) return bad(p, "precision must be 32 or 64");
+  p->prec = o.precision;
+  p->device = o.device;
+  p->steps_per_graph = std::max(0, o.steps_per_graph);
+  p->nscen = nscen;
+  CKP(p, cudaSetDevice(o.device));
+  CKP(p, cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+
+  const shm_run& r0 = runs[0];
+  if (!(r0.dt > 0) || r0.nft < 1 || (r0.nn_first != 1 && r0.nn_first != 2))
+    return bad(p, "run: dt > 0, nft >= 1, nn_first in {1,2} required");
+  for (int s = 1; s < nscen; ++s) {
+    const shm_run& r = runs[s];
+    if (r.dt != r0.dt || r.nft != r0.nft || r.nn_first != r0.nn_first || r.eta_xy != r0.eta_xy ||
+        r.eta_z != r0.eta_z || r.frm_int != r0.frm_int || r.frame_dof != r0.frame_dof)
+      return bad(p, "all scenarios of a batch must share dt, nft, nn_first, damping and frame settings");
+  }
+  p->dt = r0.dt;
+  p->nft = r0.nft;
+  p->nn_first = r0.nn_first;
+  p->nn = r0.nn_first;
+  // central-difference coefficients (main_flat_shell.m:575-604)
+  p->a0 = 1.0 / (r0.dt * r0.dt);
+  p->a1 = 1.0 / (2.0 * r0.dt);
+  const double eta[5] = {r0.eta_xy, 0.0, r0.eta_xy, 0.0, r0.eta_z};
+  for (int f = 0; f < 5; ++f) {
+    const double den = p->a0 + p->a1 * eta[f];
+    p->k1[f] = (p->a0 - p->a1 * eta[f]) / den;
+    p->k2[f] = 1.0 / den;
+  }
+  p->frm_int = r0.frm_int > 0 ? r0.frm_int : 0;
+  if (p->frm_int > 0) {
+    if (r0.frame_dof < 1 || r0.frame_dof > 5) return bad(p, "frame_dof must be 1..5");
+    p->frame_field = r0.frame_dof - 1;
+    p->nframes = r0.nft / p->frm_int;
+  }
+  p->blowup = 10.0 * r0.h;
+  if (!(r0.h > 0)) p->blowup = INFINITY;
+
+  // sizes and offsets
+  p->node_off.assign(nscen + 1, 0);
+  p->elem_off.assign(nscen + 1, 0);
+  for (int s = 0; s < nscen; ++s) {
+    const shm_mesh& m = meshes[s];
+    if (m.npe != NPE) return bad(p, "npe must be 36 (order-5 elements)");
+    if (m.fen < 1 || m.nnode < 1 || !m.nodes || !m.coords) return bad(p, "mesh: empty or NULL arrays");
+    p->node_off[s + 1] = p->node_off[s] + m.nnode;
+    p->elem_off[s + 1] = p->elem_off[s] + m.fen;
+  }
+  p->nnode = p->node_off[nscen];
+  p->fen = p->elem_off[nscen];
+  if (p->nnode > INT32_MAX / 2 || p->fen * NPE > INT32_MAX / 2) return bad(p, "mesh too large for 32-bit slots");
+  p->fen_pad = (p->fen + CTA_ELEMS - 1) / CTA_ELEMS * CTA_ELEMS;
+  p->nnode_pad = (p->nnode + 31) / 32 * 32;
+
+  // GLL constants
+  std::vector<double> gx, gw, D;
+  gll_setup(NP, gx, gw, D);
+  {
+    float D32[36], w32[6];
+    for (int i = 0; i < 36; ++i) D32[i] = (float)D[i];
+    for (int i = 0; i < 6; ++i) w32[i] = (float)gw[i];
+    CKP(p, cudaMemcpyToSymbol(c_D64, D.data(), sizeof(double) * 36));
+    CKP(p, cudaMemcpyToSymbol(c_D32, D32, sizeof(float) * 36));
+    CKP(p, cudaMemcpyToSymbol(c_w64, gw.data(), sizeof(double) * 6));
+    CKP(p, cudaMemcpyToSymbol(c_w32, w32, sizeof(float) * 6));
+  }
+
+  // connectivity, geometry, materials, slots
+  const int64_t FP = p->fen_pad;
+  std::vector<int> conn((size_t)NPE * FP, 0);
+  std::vector<double> geo((size_t)5 * NPE * FP, 0.0);
+  std::vector<int> emat(FP, 0);
+  std::vector<double> ekeep(FP, 1.0);
+  std::vector<double> mat;
+  std::vector<double> elem_m11(p->fen), elem_I11(p->fen);
+  std::vector<int> nslot_node(p->nnode + 1, 0);
+  std::vector<std::vector<int>> node_slots_tmp;  // filled below via baskets
+  std::vector<int> row_ptr(p->nnode + 1, 0), slots;
+  int mat_base = 0;
+  // per scenario
+  std::vector<std::pair<int64_t, int>> dummy;
+  std::vector<int> slot_list_sizes;
+  // gather basket-ordered slot lists per node
+  std::vector<int> node_cnt(p->nnode, 0);
+  std::vector<int64_t> node_first(p->nnode + 1, 0);
+  std::vector<int> tmp_slots;  // filled in node order later
+  std::vector<std::vector<int>> per_node;  // avoided for memory: two-pass below
+  // pass 1: count element copies per node
+  for (int s = 0; s < nscen; ++s) {
+    const shm_mesh& m = meshes[s];
+    for (int c = 0; c < NPE; ++c)
+      for (int e = 0; e < m.fen; ++e) {
+        const int nd = m.nodes[(int64_t)c * m.fen + e];
+        if (nd < 1 || nd > m.nnode) return bad(p, "mesh: node number out of range");
+        node_cnt[p->node_off[s] + nd - 1]++;
+      }
+  }
+  int nforce_tot = 0;
+  for (int s = 0; s < nscen; ++s) {
+    if (runs[s].n_force < 0 || (runs[s].n_force > 0 && (!runs[s].force_dof || !runs[s].force_val)))
+      return bad(p, "run: bad excitation arrays");
+    for (int q = 0; q < runs[s].n_force; ++q) {
+      const int d = runs[s].force_dof[q];
+      if (d < 1 || d > 5 * meshes[s].nnode) return bad(p, "run: force DOF out of range");
+      node_cnt[p->node_off[s] + (d - 1) / 5]++;
+    }
+    nforce_tot += runs[s].n_force;
+  }
+  p->nforce = nforce_tot;
+  for (int64_t g = 0; g < p->nnode; ++g) row_ptr[g + 1] = row_ptr[g] + node_cnt[g];
+  slots.assign(row_ptr[p->nnode], 0);
+  std::vector<int> fillc(p->nnode, 0);
+  const int64_t P36 = (int64_t)NPE * FP;
+  p->plane = P36 + std::max(nforce_tot, 1);
+  p->plane = (p->plane + 31) / 32 * 32;
+
+  std::vector<int> fq_field, fq_scen;
+  std::vector<double> fq_val;
+  int fq = 0;
+  for (int s = 0; s < nscen; ++s) {
+    const shm_mesh& m = meshes[s];
+    const shm_material& mt = mats[s];
+    const int64_t e0 = p->elem_off[s], n0 = p->node_off[s];
+    if (mt.nmat < 1 || !mt.table) return bad(p, "material: empty table");
+    for (int q = 0; q < mt.nmat; ++q) {
+      for (int k = 0; k < SHM_MAT_STRIDE; ++k) mat.push_back(mt.table[(int64_t)q * SHM_MAT_STRIDE + k]);
+      mat.push_back(0.0);
+    }
+    for (int e = 0; e < m.fen; ++e) {
+      const int mi = mt.elem_mat ? mt.elem_mat[e] : 0;
+      if (mi < 0 || mi >= mt.nmat) return bad(p, "material: elem_mat out of range");
+      emat[e0 + e] = mat_base + mi;
+      ekeep[e0 + e] = mt.elem_keep ? mt.elem_keep[e] : 1.0;
+      elem_m11[e0 + e] = mt.table[(int64_t)mi * SHM_MAT_STRIDE + 21];
+      elem_I11[e0 + e] = mt.table[(int64_t)mi * SHM_MAT_STRIDE + 22];
+    }
+    mat_base += mt.nmat;
+    // connectivity and geometry (main_flat_shell.m:309-350, 400-419)
+    for (int e = 0; e < m.fen; ++e) {
+      double X[NPE], Y[NPE];
+      for (int c = 0; c < NPE; ++c) {
+        const int nd = m.nodes[(int64_t)c * m.fen + e];
+        conn[(int64_t)c * FP + e0 + e] = (int)(n0 + nd - 1);
+        X[c] = m.coords[nd - 1];
+        Y[c] = m.coords[(int64_t)m.nnode + nd - 1];
+      }
+      for (int k = 0; k < NP; ++k)
+        for (int i = 0; i < NP; ++i) {
+          double J11 = 0, J21 = 0, J12 = 0, J22 = 0;
+          for (int q = 0; q < NP; ++q) {
+            J11 += D[i * NP + q] * X[k * NP + q];
+            J21 += D[i * NP + q] * Y[k * NP + q];
+            J12 += D[k * NP + q] * X[q * NP + i];
+            J22 += D[k * NP + q] * Y[q * NP + i];
+          }
+          const double det = J11 * J22 - J12 * J21;
+          if (!(det > 0)) return bad(p, "mesh: non-positive Jacobian determinant (element " + std::to_string(e + 1) + ")");
+          const int c = k * NP + i;
+          const int64_t base = (int64_t)c * FP + e0 + e;
+          geo[0 * NPE * FP + base] = J22 / det;
+          geo[1 * NPE * FP + base] = -J12 / det;
+          geo[2 * NPE * FP + base] = -J21 / det;
+          geo[3 * NPE * FP + base] = J11 / det;
+          geo[4 * NPE * FP + base] = gw[i] * gw[k] * det;
+        }
+    }
+    // assembly order: the 12-basket maps (given or built), basket by basket
+    std::vector<int> IG, IL;
+    int rows = 0;
+    if (m.basket_rows > 0 && m.I_G && m.I_L) {
+      rows = m.basket_rows;
+      IG.assign(m.I_G, m.I_G + (size_t)rows * 12);
+      IL.assign(m.I_L, m.I_L + (size_t)rows * 12);
+    } else {
+      build_baskets(m.fen, NPE, m.nnode, m.nodes, IG, IL, rows);
+    }
+    for (int b = 0; b < 12; ++b)
+      for (int r = 0; r < rows; ++r) {
+        const int kg = IG[(size_t)b * rows + r], kl = IL[(size_t)b * rows + r];
+        if (kg == 0) continue;
+        if (kg < 1 || kg > m.nnode || kl < 1 || kl > m.fen * NPE) return bad(p, "mesh: basket map out of range");
+        const int e = (kl - 1) / NPE, c = (kl - 1) % NPE;
+        const int64_t g = n0 + kg - 1;
+        if (fillc[g] >= node_cnt[g]) return bad(p, "mesh: basket maps inconsistent with nodes");
+        slots[row_ptr[g] + fillc[g]++] = (int)(c * FP + e0 + e);
+      }
+    // excitation slots after the element slots
+    for (int q = 0; q < runs[s].n_force; ++q) {
+      const int d = runs[s].force_dof[q];
+      const int64_t g = n0 + (d - 1) / 5;
+      if (fillc[g] >= node_cnt[g]) return bad(p, "internal: slot overflow");
+      slots[row_ptr[g] + fillc[g]++] = (int)(P36 + fq);
+      fq_field.push_back((d - 1) % 5);
+      fq_scen.push_back(s);
+      fq_val.push_back(runs[s].force_val[q]);
+      ++fq;
+    }
+  }
+  for (int64_t g = 0; g < p->nnode; ++g)
+    if (fillc[g] != node_cnt[g]) return bad(p, "mesh: basket maps do not cover every element node");
+
+  // diagonal mass (main_flat_shell.m:493-501), summed in basket order
+  std::vector<double> minv((size_t)2 * p->nnode_pad, 0.0);
+  p->mass.assign((size_t)5 * p->nnode, 0.0);
+  for (int64_t g = 0; g < p->nnode; ++g) {
+    double mt_ = 0, mr_ = 0;
+    for (int q = row_ptr[g]; q < row_ptr[g + 1]; ++q) {
+      const int64_t sl = slots[q];
+      if (sl >= P36) continue;
+      const int64_t c = sl / FP, e = sl % FP;
+      const double W = geo[4 * NPE * FP + c * FP + e];
+      mt_ += W * elem_m11[e];
+      mr_ += W * elem_I11[e];
+    }
+    minv[g] = mt_ > 0 ? 1.0 / mt_ : 0.0;
+    minv[p->nnode_pad + g] = mr_ > 0 ? 1.0 / mr_ : 0.0;
+    p->mass[5 * g + 0] = mt_;
+    p->mass[5 * g + 1] = mr_;
+    p->mass[5 * g + 2] = mt_;
+    p->mass[5 * g + 3] = mr_;
+    p->mass[5 * g + 4] = mt_;
+  }
+
+  // outputs and sensors
+  std::vector<int> out_node, out_field, esens(FP, -1), sptr(1, 0);
+  p->out_off.assign(nscen + 1, 0);
+  p->sens_off.assign(nscen + 1, 0);
+  for (int s = 0; s < nscen; ++s) {
+    const shm_run& r = runs[s];
+    for (int q = 0; q < r.n_out; ++q) {
+      const int d = r.out_dof[q];
+      if (d < 1 || d > 5 * meshes[s].nnode) return bad(p, "run: output DOF out of range");
+      out_node.push_back((int)(p->node_off[s] + (d - 1) / 5));
+      out_field.push_back((d - 1) % 5);
+    }
+    p->out_off[s + 1] = p->out_off[s] + r.n_out;
+    for (int k = 0; k < r.n_sens; ++k) {
+      for (int q = r.sens_ptr[k]; q < r.sens_ptr[k + 1]; ++q) {
+        const int e = r.sens_el[q];
+        if (e < 0 || e >= meshes[s].fen) return bad(p, "run: sensor element out of range");
+        if (esens[p->elem_off[s] + e] >= 0) return bad(p, "run: element listed in two sensors");
+        esens[p->elem_off[s] + e] = p->nslot++;
+      }
+      sptr.push_back(p->nslot);
+    }
+    p->sens_off[s + 1] = p->sens_off[s] + r.n_sens;
+    if (r.n_sens > 0) {
+      if (!(r.g33 != 0)) return bad(p, "run: g33 must be nonzero with sensors");
+      p->sc_k0 = r.pzt_thickness / r.g33;
+      p->sc_e31 = r.e31;
+      p->sc_e32 = r.e32;
+      p->sc_hh = r.h / 2;
+    }
+  }
+  p->nout = p->out_off[nscen];
+  p->nsens = p->sens_off[nscen];
+
+  shm_status st;
+  if ((st = (p->prec == 64 ? build_device<double>(p, conn, geo, emat, ekeep, mat, minv)
+                           : build_device<float>(p, conn, geo, emat, ekeep, mat, minv))) != SHM_OK)
+    return st;
+  if ((st = upload(p, &p->row_ptr, row_ptr)) != SHM_OK) return st;
+  if ((st = upload(p, &p->slots, slots)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_field, fq_field)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_scen, fq_scen)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_val, fq_val)) != SHM_OK) return st;
+  if ((st = upload(p, &p->out_node, out_node)) != SHM_OK) return st;
+  if ((st = upload(p, &p->out_field, out_field)) != SHM_OK) return st;
+  if ((st = upload(p, &p->esens, esens)) != SHM_OK) return st;
+  if ((st = upload(p, &p->sptr, sptr)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->st, (size_t)nscen * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->displ, (size_t)std::max(p->nout, 1) * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->vsum, (size_t)std::max(p->nslot, 1) * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->volt, (size_t)std::max(p->nsens, 1) * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->flag, 4)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->d_base, 4)) != SHM_OK) return st;
+  if ((st = set_func_attrs(p)) != SHM_OK) return st;
+
+  // path selection
+  p->path = 1;
+  if (o.path == 2 || o.path == 0) {
+    std::string why;
+    shm_status ss = struct_build(p, nscen, meshes, mats, runs, o.tile_elems, gw, geo, emat, ekeep, esens, fq_field,
+                                 fq_val, why);
+    if (ss == SHM_OK) {
+      p->path = 2;
+    } else if (o.path == 2) {
+      p->err = "structured path not available: " + why;
+      return ss == SHM_ERR_OOM || ss == SHM_ERR_CUDA ? ss : SHM_ERR_UNSUPPORTED;
+    }
+  }
+  CKP(p, cudaDeviceSynchronize());
+  return shm_reset(p);
+}
+
+// helper used by the structured builder to register device allocations
+extern "C" void* shm__plan_alloc(void* plan, size_t bytes) {
+  shm_plan* p = (shm_plan*)plan;
+  void* q = nullptr;
+  if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+  cudaMemset(q, 0, std::max<size_t>(bytes, 16));
+  p->allocs.push_back(q);
+  return q;
+}
+
+extern "C" shm_status shm_plan_destroy(shm_plan* p) {
+  if (!p) return SHM_OK;
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  for (void* q : p->allocs) cudaFree(q);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+  return SHM_OK;
+}
+
+extern "C" const char* shm_last_error(const shm_plan* p) { return p ? p->err.c_str() : "no plan"; }
+
+static cudaStream_t pick_stream(shm_plan* p, void* stream) {
+  return stream ? (cudaStream_t)stream : p->stream;
+}
+
+extern "C" shm_status shm_reset(shm_plan* p) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  cudaStream_t s = p->stream;
+  const size_t ts = p->prec == 64 ? 8 : 4;
+  CKP(p, cudaMemsetAsync(p->UA, 0, ts * 5 * p->nnode_pad, s));
+  CKP(p, cudaMemsetAsync(p->UB, 0, ts * 5 * p->nnode_pad, s));
+  if (p->frames) CKP(p, cudaMemsetAsync(p->frames, 0, ts * p->nframes * p->nnode_pad, s));
+  CKP(p, cudaMemsetAsync(p->displ, 0, sizeof(double) * std::max(p->nout, 1) * p->nft, s));
+  CKP(p, cudaMemsetAsync(p->vsum, 0, sizeof(double) * std::max(p->nslot, 1) * p->nft, s));
+  CKP(p, cudaMemsetAsync(p->flag, 0, 4, s));
+  CKP(p, cudaMemcpyAsync(p->d_base, &p->nn_first, 4, cudaMemcpyHostToDevice, s));
+  CKP(p, cudaStreamSynchronize(s));
+  p->nn = p->nn_first;
+  p->ran = false;
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_set_signal(shm_plan* p, const double* st, void* stream) {
+  if (!p || !st) return SHM_ERR_BAD_ARG;
+  cudaStream_t s = pick_stream(p, stream);
+  CKP(p, cudaMemcpyAsync(p->st, st, sizeof(double) * p->nscen * p->nft, cudaMemcpyHostToDevice, s));
+  return SHM_OK;
+}
+
+static shm_status ensure_graph(shm_plan* p, cudaStream_t s) {
+  if (p->steps_per_graph <= 0 || p->gexec) return SHM_OK;
+  cudaGraph_t g = nullptr;
+  CKP(p, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < p->steps_per_graph; ++k) {
+    cudaError_t e = launch_step(p, k, s);
+    if (e != cudaSuccess) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      p->err = std::string("capture: ") + cudaGetErrorString(e);
+      return SHM_ERR_CUDA;
+    }
+  }
+  k_advance<<<1, 1, 0, s>>>(p->d_base, p->steps_per_graph);
+  CKP(p, cudaStreamEndCapture(s, &g));
+  cudaError_t e = cudaGraphInstantiate(&p->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    p->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+    p->gexec = nullptr;
+    return SHM_ERR_CUDA;
+  }
+  p->gsteps = p->steps_per_graph;
+  return SHM_OK;
+}
+
+static shm_status advance_async(shm_plan* p, int nsteps, cudaStream_t s) {
+  if (nsteps < 0) return bad(p, "nsteps < 0");
+  if (p->nn + nsteps > p->nft + 1) return bad(p, "advance past nft");
+  shm_status st = ensure_graph(p, s);
+  if (st != SHM_OK) return st;
+  int left = nsteps;
+  while (p->gexec && left >= p->gsteps) {
+    CKP(p, cudaGraphLaunch(p->gexec, s));
+    left -= p->gsteps;
+  }
+  if (left > 0) {
+    for (int k = 0; k < left; ++k) CKP(p, launch_step(p, k, s));
+    k_advance<<<1, 1, 0, s>>>(p->d_base, left);
+    CKP(p, cudaGetLastError());
+  }
+  p->nn += nsteps;
+  p->ran = true;
+  return SHM_OK;
+}
+
+static shm_status check_flag(shm_plan* p, cudaStream_t s) {
+  int flag = 0;
+  CKP(p, cudaMemcpyAsync(&flag, p->flag, 4, cudaMemcpyDeviceToHost, s));
+  CKP(p, cudaStreamSynchronize(s));
+  if (flag) {
+    p->err = "integration error: blow-up or non-finite state detected";
+    return SHM_ERR_DIVERGED;
+  }
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_advance(shm_plan* p, int32_t nsteps, void* stream) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  cudaStream_t s = pick_stream(p, stream);
+  shm_status st = advance_async(p, nsteps, s);
+  if (st != SHM_OK) return st;
+  return check_flag(p, s);
+}
+
+extern "C" shm_status shm_time_steps(shm_plan* p, int32_t nsteps, float* ms) {
+  if (!p || !ms) return SHM_ERR_BAD_ARG;
+  cudaStream_t s = p->stream;
+  cudaEvent_t e0, e1;
+  CKP(p, cudaEventCreate(&e0));
+  CKP(p, cudaEventCreate(&e1));
+  CKP(p, cudaStreamSynchronize(s));
+  CKP(p, cudaEventRecord(e0, s));
+  shm_status st = advance_async(p, nsteps, s);
+  if (st != SHM_OK) return st;
+  CKP(p, cudaEventRecord(e1, s));
+  CKP(p, cudaEventSynchronize(e1));
+  CKP(p, cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return check_flag(p, s);
+}
+
+template <typename T>
+static void to_host_frames(const std::vector<T>& dev, shm_plan* p, double* frames) {
+  // device [nframes][nnode_pad] over all scenarios -> [nscen][nframes][nnode_s]
+  double* o = frames;
+  for (int s = 0; s < p->nscen; ++s) {
+    const int64_t n0 = p->node_off[s], nn = p->node_off[s + 1] - n0;
+    for (int c = 0; c < p->nframes; ++c)
+      for (int64_t g = 0; g < nn; ++g) *o++ = (double)dev[(size_t)c * p->nnode_pad + n0 + g];
+  }
+}
+
+extern "C" shm_status shm_read_outputs(shm_plan* p, double* displ, double* voltage, double* frames,
+                                       void* stream) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  cudaStream_t s = pick_stream(p, stream);
+  if (displ && p->nout > 0)
+    CKP(p, cudaMemcpyAsync(displ, p->displ, sizeof(double) * p->nout * p->nft, cudaMemcpyDeviceToHost, s));
+  if (voltage && p->nsens > 0) {
+    const int n = p->nsens * p->nft;
+    k_voltage<<<(n + 255) / 256, 256, 0, s>>>(p->vsum, p->sptr, p->volt, p->nsens, p->nft);
+    CKP(p, cudaGetLastError());
+    CKP(p, cudaMemcpyAsync(voltage, p->volt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  }
+  if (frames && p->nframes > 0) {
+    const size_t cnt = (size_t)p->nframes * p->nnode_pad;
+    if (p->prec == 64) {
+      std::vector<double> h(cnt);
+      CKP(p, cudaMemcpyAsync(h.data(), p->frames, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
+      CKP(p, cudaStreamSynchronize(s));
+      to_host_frames(h, p, frames);
+    } else {
+      std::vector<float> h(cnt);
+      CKP(p, cudaMemcpyAsync(h.data(), p->frames, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s));
+      CKP(p, cudaStreamSynchronize(s));
+      to_host_frames(h, p, frames);
+    }
+  }
+  CKP(p, cudaStreamSynchronize(s));
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_forward(shm_plan* p, const double* st, double* displ, double* voltage, double* frames,
+                                  void* stream) {
+  if (!p || !st) return SHM_ERR_BAD_ARG;
+  shm_status r = shm_reset(p);
+  if (r != SHM_OK) return r;
+  cudaStream_t s = pick_stream(p, stream);
+  if ((r = shm_set_signal(p, st, s)) != SHM_OK) return r;
+  const int nsteps = p->nft - p->nn_first + 1;
+  if ((r = advance_async(p, nsteps, s)) != SHM_OK) return r;
+  shm_status div = check_flag(p, s);
+  if ((r = shm_read_outputs(p, displ, voltage, frames, s)) != SHM_OK) return r;
+  return div;
+}
+
+// state transfer in the reference layout [nnode][5]
+template <typename T>
+static shm_status get_state_t(shm_plan* p, double* U, double* uold) {
+  const bool odd = ((p->nn - p->nn_first) & 1);
+  std::vector<T> h((size_t)5 * p->nnode_pad);
+  for (int which = 0; which < 2; ++which) {
+    double* out = which == 0 ? U : uold;
+    if (!out) continue;
+    const void* src = (which == 0) ? (odd ? p->UB : p->UA) : (odd ? p->UA : p->UB);
+    CKP(p, cudaMemcpy(h.data(), src, sizeof(T) * h.size(), cudaMemcpyDeviceToHost));
+    for (int64_t g = 0; g < p->nnode; ++g)
+      for (int f = 0; f < 5; ++f) out[5 * g + f] = (double)h[(size_t)f * p->nnode_pad + g];
+  }
+  return SHM_OK;
+}
+
+template <typename T>
+static shm_status set_state_t(shm_plan* p, const double* U, const double* uold, int nn) {
+  p->nn = nn;
+  CKP(p, cudaMemcpy(p->d_base, &nn, 4, cudaMemcpyHostToDevice));
+  const bool odd = ((nn - p->nn_first) & 1);
+  std::vector<T> h((size_t)5 * p->nnode_pad, T(0));
+  for (int which = 0; which < 2; ++which) {
+    const double* in = which == 0 ? U : uold;
+    std::fill(h.begin(), h.end(), T(0));
+    if (in)
+      for (int64_t g = 0; g < p->nnode; ++g)
+        for (int f = 0; f < 5; ++f) h[(size_t)f * p->nnode_pad + g] = (T)in[5 * g + f];
+    void* dst = (which == 0) ? (odd ? p->UB : p->UA) : (odd ? p->UA : p->UB);
+    CKP(p, cudaMemcpy(dst, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  }
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_get_state(shm_plan* p, double* U, double* uold) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  CKP(p, cudaStreamSynchronize(p->stream));
+  return p->prec == 64 ? get_state_t<double>(p, U, uold) : get_state_t<float>(p, U, uold);
+}
+
+extern "C" shm_status shm_set_state(shm_plan* p, const double* U, const double* uold, int32_t nn) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (nn < p->nn_first || nn > p->nft + 1) return bad(p, "set_state: nn out of range");
+  CKP(p, cudaStreamSynchronize(p->stream));
+  return p->prec == 64 ? set_state_t<double>(p, U, uold, nn) : set_state_t<float>(p, U, uold, nn);
+}
+
+template <typename T>
+static shm_status apply_k_t(shm_plan* p, const double* U, double* F) {
+  // uses the general element kernel on a temporary copy, whatever the path
+  std::vector<T> h((size_t)5 * p->nnode_pad, T(0));
+  for (int64_t g = 0; g < p->nnode; ++g)
+    for (int f = 0; f < 5; ++f) h[(size_t)f * p->nnode_pad + g] = (T)U[5 * g + f];
+  T* dU = nullptr;
+  T* dOut = nullptr;
+  int* dbase = nullptr;
+  CKP(p, cudaMalloc(&dU, sizeof(T) * h.size()));
+  CKP(p, cudaMalloc(&dOut, sizeof(T) * h.size()));
+  CKP(p, cudaMalloc(&dbase, 4));
+  CKP(p, cudaMemcpy(dU, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  CKP(p, cudaMemcpy(dbase, &p->nn_first, 4, cudaMemcpyHostToDevice));
+  GenArgs<T> a = make_args<T>(p);
+  a.UA = dU;
+  a.UB = dU;
+  a.nforce = 0;
+  a.nout = 0;
+  a.d_base = dbase;
+  const int nblk = (int)(p->fen_pad / CTA_ELEMS);
+  k_elem_general<T, false><<<nblk, CTA_THREADS, elem_smem_bytes(sizeof(T) == 8 ? 64 : 32), p->stream>>>(a, 0);
+  k_assemble_only<T><<<(int)((p->nnode + 255) / 256), 256, 0, p->stream>>>(a, dOut);
+  CKP(p, cudaGetLastError());
+  CKP(p, cudaMemcpyAsync(h.data(), dOut, sizeof(T) * h.size(), cudaMemcpyDeviceToHost, p->stream));
+  CKP(p, cudaStreamSynchronize(p->stream));
+  for (int64_t g = 0; g < p->nnode; ++g)
+    for (int f = 0; f < 5; ++f) F[5 * g + f] = (double)h[(size_t)f * p->nnode_pad + g];
+  cudaFree(dU);
+  cudaFree(dOut);
+  cudaFree(dbase);
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_apply_stiffness(shm_plan* p, const double* U, double* F) {
+  if (!p || !U || !F) return SHM_ERR_BAD_ARG;
+  CKP(p, cudaStreamSynchronize(p->stream));
+  return p->prec == 64 ? apply_k_t<double>(p, U, F) : apply_k_t<float>(p, U, F);
+}
+
+extern "C" shm_status shm_plan_info(const shm_plan* p, int64_t* info) {
+  if (!p || !info) return SHM_ERR_BAD_ARG;
+  info[0] = p->nnode;
+  info[1] = p->fen;
+  info[2] = 5 * p->nnode;
+  info[3] = p->path;
+  info[4] = p->prec;
+  info[5] = p->nframes;
+  info[6] = p->path == 2 ? 1 : 2;
+  info[7] = p->path == 2 ? p->sp.tile : 0;
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_mass(shm_plan* p, double* mg) {
+  if (!p || !mg) return SHM_ERR_BAD_ARG;
+  std::memcpy(mg, p->mass.data(), sizeof(double) * p->mass.size());
+  return SHM_OK;
+}

@@ -1,0 +1,319 @@
+"""Host side of the engine: plans, scenarios and the reference's solver entry point.
+
+``main_flat_shell`` mirrors the reference's
+``t_frames = main_flat_shell(test_case, input_no, meshfile, mode, output_name, tasks)``
+(src/models/flat_shell/flat_shell_engine/main_flat_shell.m:1) and its output
+layout (displ<N>.mat, voltage<N>.mat, time<N>.mat, V?_frame<c>.mat).  The time
+loop itself runs in libshmsem.so on the GPU; this module only prepares inputs
+and writes results.  There is no CPU path: ``mode`` other than 'gpu' raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+from .materials import table_row
+
+FIELD_NAMES = ("x", "Fix", "y", "Fiy", "z")  # DOF order u, phi_x, v, phi_y, w
+
+
+@dataclass
+class Scenario:
+    """One plate: mesh, laminate per element, excitation and outputs."""
+    mesh: dict                       # nodes [fen,36] 1-based, coords [nnode,3], optional nex/ney, I_G/I_L
+    mat_table: np.ndarray            # [nmat, 23]
+    elem_mat: np.ndarray | None = None
+    elem_keep: np.ndarray | None = None
+    force_dof: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))   # 1-based DOF
+    force_val: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    out_dof: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))     # 1-based DOF
+    sensors: list = field(default_factory=list)   # list of 0-based element arrays (PZT sensors)
+    pzt: dict | None = None          # pzt_thickness, g33, e31, e32
+    signal: np.ndarray | None = None  # st [nft]
+
+
+@dataclass
+class RunConfig:
+    dt: float
+    nft: int
+    nn_first: int = 2
+    eta_xy: float = 0.0
+    eta_z: float = 0.0
+    h: float = 0.0
+    frm_int: int = 0
+    frame_dof: int = 5
+
+
+class Plan:
+    """A set of scenarios advanced together on one GPU (owns the C plan)."""
+
+    def __init__(self, scenarios, run: RunConfig, precision: int = 64, path: int = 0,
+                 steps_per_graph: int = 0, tile_elems: int = 0, device: int = 0):
+        self.lib = native.load()
+        self.scenarios = list(scenarios)
+        self.run = run
+        self._keep = []  # arrays referenced by the C structs during creation
+        n = len(self.scenarios)
+        meshes = (native.ShmMesh * n)()
+        mats = (native.ShmMaterial * n)()
+        runs = (native.ShmRun * n)()
+        for i, sc in enumerate(self.scenarios):
+            self._fill(sc, meshes[i], mats[i], runs[i])
+        opt = native.ShmOptions(precision, path, steps_per_graph, tile_elems, device)
+        handle = C.c_void_p()
+        st = self.lib.shm_plan_create(n, meshes, mats, runs, C.byref(opt), C.byref(handle))
+        self.handle = handle
+        if st != native.SHM_OK:
+            msg = self.lib.shm_last_error(handle).decode() if handle.value else ""
+            self.lib.shm_plan_destroy(handle)
+            self.handle = None
+            raise native.ShmError(st, msg)
+        self._keep.clear()
+        info = (C.c_int64 * 8)()
+        self.lib.shm_plan_info(self.handle, info)
+        self.info = dict(nnode=info[0], fen=info[1], ndof=info[2], path=info[3], precision=info[4],
+                         nframes=info[5], launches_per_step=info[6], tile=info[7])
+        self.nscen = n
+        self.nft = run.nft
+
+    def _arr(self, a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self._keep.append(a)
+        return a
+
+    def _fill(self, sc: Scenario, m, mt, r):
+        mesh = sc.mesh
+        nodes = self._arr(np.asarray(mesh["nodes"]).T, np.int32)   # column-major [fen x npe]
+        coords = self._arr(np.asarray(mesh["coords"], float).T, np.float64)
+        fen, npe = np.asarray(mesh["nodes"]).shape
+        m.fen, m.npe, m.nnode = fen, npe, np.asarray(mesh["coords"]).shape[0]
+        m.nodes = native.ptr(nodes, native.I32P)
+        m.coords = native.ptr(coords)
+        if mesh.get("I_G") is not None:
+            IG = self._arr(np.asarray(mesh["I_G"]).T, np.int32)
+            IL = self._arr(np.asarray(mesh["I_L"]).T, np.int32)
+            m.basket_rows = np.asarray(mesh["I_G"]).shape[0]
+            m.I_G, m.I_L = native.ptr(IG, native.I32P), native.ptr(IL, native.I32P)
+        else:
+            m.basket_rows = 0
+        m.grid_nex = int(mesh.get("nex", 0)) if mesh.get("structured", True) else 0
+        m.grid_ney = int(mesh.get("ney", 0)) if mesh.get("structured", True) else 0
+        tab = self._arr(np.atleast_2d(sc.mat_table), np.float64)
+        mt.nmat = tab.shape[0]
+        mt.table = native.ptr(tab)
+        mt.elem_mat = native.ptr(self._arr(sc.elem_mat, np.int32), native.I32P) if sc.elem_mat is not None else None
+        mt.elem_keep = native.ptr(self._arr(sc.elem_keep, np.float64)) if sc.elem_keep is not None else None
+        run = self.run
+        r.dt, r.nft, r.nn_first = run.dt, run.nft, run.nn_first
+        r.eta_xy, r.eta_z = run.eta_xy, run.eta_z
+        fd = self._arr(sc.force_dof, np.int32)
+        fv = self._arr(sc.force_val, np.float64)
+        r.n_force, r.force_dof, r.force_val = len(fd), native.ptr(fd, native.I32P), native.ptr(fv)
+        od = self._arr(sc.out_dof, np.int32)
+        r.n_out, r.out_dof = len(od), native.ptr(od, native.I32P)
+        if sc.sensors:
+            ptrs = np.zeros(len(sc.sensors) + 1, np.int32)
+            ptrs[1:] = np.cumsum([len(s) for s in sc.sensors])
+            els = np.concatenate([np.asarray(s, np.int32) for s in sc.sensors])
+            r.n_sens = len(sc.sensors)
+            r.sens_ptr = native.ptr(self._arr(ptrs, np.int32), native.I32P)
+            r.sens_el = native.ptr(self._arr(els, np.int32), native.I32P)
+            p = sc.pzt
+            r.pzt_thickness, r.g33, r.e31, r.e32 = p["pzt_thickness"], p["g33"], p["e31"], p["e32"]
+        else:
+            r.n_sens = 0
+        r.h = run.h
+        r.frm_int, r.frame_dof = run.frm_int, run.frame_dof
+
+    # ------------------------------------------------------------------
+    def _check(self, st):
+        native.check(self.lib, self.handle, st)
+
+    def close(self):
+        if self.handle is not None:
+            self.lib.shm_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def signals(self):
+        return np.stack([np.asarray(sc.signal, float) for sc in self.scenarios])
+
+    def forward(self, signals=None, want_frames=False):
+        """Whole MAIN LOOP for every scenario; returns per-scenario outputs."""
+        st = np.ascontiguousarray(self.signals() if signals is None else signals, dtype=np.float64)
+        nout = sum(len(s.out_dof) for s in self.scenarios)
+        nsens = sum(len(s.sensors) for s in self.scenarios)
+        displ = np.zeros(max(nout, 1) * self.nft)
+        volt = np.zeros(max(nsens, 1) * self.nft)
+        nfr = self.info["nframes"]
+        frames = np.zeros(max(nfr * self.info["nnode"], 1)) if (want_frames and nfr) else None
+        self._check(self.lib.shm_forward(self.handle, native.ptr(st), native.ptr(displ), native.ptr(volt),
+                                         native.ptr(frames), None))
+        return self._split(displ, volt, frames)
+
+    def _split(self, displ, volt, frames):
+        out = []
+        o = s_ = fo = 0
+        for sc in self.scenarios:
+            no, ns = len(sc.out_dof), len(sc.sensors)
+            nnode = np.asarray(sc.mesh["coords"]).shape[0]
+            d = displ[o * self.nft:(o + no) * self.nft].reshape(no, self.nft).T.copy()
+            v = volt[s_ * self.nft:(s_ + ns) * self.nft].reshape(ns, self.nft).T.copy()
+            res = dict(displ=d, voltage=v)
+            if frames is not None:
+                nfr = self.info["nframes"]
+                res["frames"] = frames[fo:fo + nfr * nnode].reshape(nfr, nnode).copy()
+                fo += nfr * nnode
+            out.append(res)
+            o += no
+            s_ += ns
+        return out
+
+    def reset(self):
+        self._check(self.lib.shm_reset(self.handle))
+
+    def set_signal(self, signals=None):
+        st = np.ascontiguousarray(self.signals() if signals is None else signals, dtype=np.float64)
+        self._check(self.lib.shm_set_signal(self.handle, native.ptr(st), None))
+
+    def advance(self, nsteps):
+        self._check(self.lib.shm_advance(self.handle, int(nsteps), None))
+
+    def time_steps(self, nsteps) -> float:
+        ms = C.c_float()
+        self._check(self.lib.shm_time_steps(self.handle, int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def read_outputs(self, want_frames=False):
+        nout = sum(len(s.out_dof) for s in self.scenarios)
+        nsens = sum(len(s.sensors) for s in self.scenarios)
+        displ = np.zeros(max(nout, 1) * self.nft)
+        volt = np.zeros(max(nsens, 1) * self.nft)
+        nfr = self.info["nframes"]
+        frames = np.zeros(max(nfr * self.info["nnode"], 1)) if (want_frames and nfr) else None
+        self._check(self.lib.shm_read_outputs(self.handle, native.ptr(displ), native.ptr(volt),
+                                              native.ptr(frames), None))
+        return self._split(displ, volt, frames)
+
+    def get_state(self):
+        n = self.info["nnode"]
+        U = np.zeros(5 * n)
+        Uo = np.zeros(5 * n)
+        self._check(self.lib.shm_get_state(self.handle, native.ptr(U), native.ptr(Uo)))
+        return U, Uo
+
+    def set_state(self, U, Uold, nn):
+        U = np.ascontiguousarray(U, np.float64)
+        Uo = np.ascontiguousarray(Uold, np.float64)
+        self._check(self.lib.shm_set_state(self.handle, native.ptr(U), native.ptr(Uo), int(nn)))
+
+    def apply_stiffness(self, U):
+        U = np.ascontiguousarray(U, np.float64)
+        F = np.zeros_like(U)
+        self._check(self.lib.shm_apply_stiffness(self.handle, native.ptr(U), native.ptr(F)))
+        return F
+
+    def mass(self):
+        mg = np.zeros(5 * self.info["nnode"])
+        self._check(self.lib.shm_mass(self.handle, native.ptr(mg)))
+        return mg
+
+
+# ----------------------------------------------------------------------
+# the reference's entry point
+# ----------------------------------------------------------------------
+
+def hanning_signal(dt, nft, f_1, f_2, t_1=0.0):
+    """Hann-windowed tone burst (Hanning_signal.m:12-23): returns t, st."""
+    t = np.arange(nft) * dt
+    t_2 = t_1 + 1.0 / f_1
+    on = (t >= t_1) & (t <= t_2)
+    st = np.where(on, 0.5 * (1 - np.cos(2 * np.pi * f_1 * (t - t_2))) * np.sin(2 * np.pi * f_2 * (t - t_1)), 0.0)
+    return t, st
+
+
+def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", output_name: str = ".",
+                    tasks=(), precision: int = 64, variant: str = "main_flat_shell"):
+    """Flat-shell forward solve with the reference's interface and outputs.
+
+    inputs: the fields of an ``inputs/input<N>.m`` script (nft, tt, f_1, f_2,
+    t_1, nFrames, field_variable, etad_xy, etad_z, V0, lh, and the laminate as
+    a material table ``mat_table`` or q11..q66 + lalpha + rho).
+    mesh:   the fields of the mesh .mat file (nodes, coords, optional I_G, I_L,
+    mesh_min, mesh_max, nex/ney for structured plates).
+    variant: 'main_flat_shell' (dt = tt/nft, loop nn = 2..nft, force at the
+    plate centre) or 'force_excit_c' (dt = tt/(nft-1), nn = 1..nft, force at
+    ``force_coords``, outputs at ``output_coords``).
+    Writes displ<test_case>.mat, time<test_case>.mat and velocity frames
+    V{x,Fix,y,Fiy,z}_frame<c>.mat (field_variable 'velocity' only) into
+    output_name; returns t_frames.
+    """
+    if mode != "gpu":
+        raise ValueError("this engine runs the time loop on the GPU only (mode='gpu')")
+    from scipy.io import savemat
+    from . import materials as M
+    from . import mesh as MS
+
+    nft = int(inputs["nft"])
+    if variant == "main_flat_shell":
+        dt, nn_first = inputs["tt"] / nft, 2
+    else:
+        dt, nn_first = inputs["tt"] / (nft - 1), 1
+    t, st = hanning_signal(dt, nft, inputs["f_1"], inputs["f_2"], inputs.get("t_1", 0.0))
+    if "mat_table" in inputs:
+        table = np.atleast_2d(inputs["mat_table"])
+        h = float(np.sum(inputs["lh"]))
+    else:
+        q = {k: inputs[k] for k in ("q11", "q12", "q22", "q44", "q55", "q66")}
+        lam = M.laminate(q, inputs["rho"], inputs["lh"], inputs["lalpha"])
+        table = table_row(lam)[None, :]
+        h = lam["h"]
+    coords = np.asarray(mesh["coords"], float)
+    if variant == "main_flat_shell":
+        cen = (np.asarray(mesh["mesh_max"]) - np.asarray(mesh["mesh_min"])) / 2
+        out_nodes = [MS.nearest_node(coords, cen[0], cen[1])]
+        force_node = out_nodes[0]
+    else:
+        out_nodes = [MS.nearest_node(coords, x, y) for x, y in np.atleast_2d(inputs["output_coords"])]
+        fc = np.atleast_2d(inputs["force_coords"])[0]
+        force_node = MS.nearest_node(coords, fc[0], fc[1])
+    nframes = int(inputs.get("nFrames", 0))
+    frm_int = nft // nframes if nframes else 0
+    fv = inputs.get("field_variable", "velocity")
+    sc = Scenario(mesh=mesh, mat_table=table, force_dof=np.array([5 * force_node], np.int32),
+                  force_val=np.array([inputs["V0"]]), out_dof=5 * np.array(out_nodes, np.int32), signal=st)
+    run = RunConfig(dt=dt, nft=nft, nn_first=nn_first, eta_xy=inputs.get("etad_xy", 0.0),
+                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int if fv == "velocity" else 0,
+                    frame_dof=5)
+    os.makedirs(output_name, exist_ok=True)
+    tic = time.perf_counter()
+    plan = Plan([sc], run, precision=precision)
+    try:
+        res = plan.forward(want_frames=(fv == "velocity" and frm_int > 0))[0]
+    finally:
+        plan.close()
+    elapsed = time.perf_counter() - tic
+    savemat(os.path.join(output_name, f"displ{test_case}.mat"), {"displ": res["displ"]})
+    n_nodes = coords.shape[0]
+    savemat(os.path.join(output_name, f"time{test_case}.mat"),
+            {"minTime": elapsed / max(nft - 1, 1), "averageTime": elapsed / max(nft - 1, 1),
+             "TotalNofNodes": n_nodes, "t": t})
+    t_frames = np.zeros(nframes)
+    if "frames" in res:
+        # frame c at loop index nn = c*frm_int; only the w velocity is computed
+        # on the device (frame_dof=5), the other components are written as in
+        # the reference only when requested through frame_dof
+        for c in range(res["frames"].shape[0]):
+            t_frames[c] = t[(c + 1) * frm_int - 1]
+            savemat(os.path.join(output_name, f"Vz_frame{c + 1}.mat"), {"Vz": res["frames"][c][:, None]})
+    return t_frames

@@ -1,0 +1,99 @@
+"""Synthetic workloads with the shapes of the engine's reference configurations.
+
+No measured or published dataset is involved; every plate, damage map and
+excitation is generated here from a seed.  Sizes:
+
+* ``plate_force``  (config "cfg1"): 0.5 m square CFRP plate, 20x20 order-5
+  elements, 5-cycle Hann 50 kHz transverse force at the centre node, free
+  edges, 0.5 ms, 8 out-of-plane outputs on a 150 mm circle.  FP64.
+* ``plate_pzt``    (config "cfg2"): 1 m plate, 200x200 elements (~1 M nodes,
+  ~5 M DOF), PZT disc 10 mm x 0.2 mm at the centre as electromechanical nodal
+  loads, 100 kHz burst, 1 ms, w-velocity frames every 100 steps, 16 outputs.
+* ``batch``        (config "cfg4"): 512 plates, side ~ U{40..80} elements of
+  6.25 mm, 1-3 elliptical damage zones with stiffness reduction U(0.2, 0.8),
+  random actuator node, carrier in {50, 75, 100} kHz, 8 outputs, 0.4 ms.  FP32.
+* ``adjoint``      (config "cfg5"): 50x50 plate, 2 500 per-element damage
+  parameters, hidden map with two zones at 0.5 reduction, 50 kHz.
+
+Damping is the reference's usual mass-proportional pair (etad_xy = 4e2,
+etad_z = 4e3 1/s, inputs/input16.m) and the time step is 0.9 x the element
+eigenvalue bound (element.stable_dt).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import element as EL
+from . import materials as M
+from . import mesh as MS
+from .solver import RunConfig, Scenario, hanning_signal
+
+ETA_XY, ETA_Z = 4e2, 4e3
+
+
+def _dt_for(ax, ay, lams):
+    return EL.stable_dt([EL.rect_nodes(ax, ay)], lams)
+
+
+def plate_force(nex=20, ney=20, L=0.5, T=0.5e-3, f=50e3, n_out=8, radius=0.15, dt=None, nft=None):
+    lam = M.cfrp_laminate()
+    mesh = MS.structured_plate(L, L, nex, ney)
+    if dt is None:
+        dt = _dt_for(L / nex, L / ney, [lam])
+    if nft is None:
+        nft = int(np.ceil(T / dt)) + 1
+    xc = yc = L / 2
+    centre = MS.nearest_node(mesh["coords"], xc, yc)
+    outs = MS.circle_sensor_nodes(mesh, xc, yc, min(radius, 0.45 * L), n_out)
+    _, st = hanning_signal(dt, nft, f / 5, f, 0.0)
+    sc = Scenario(mesh=mesh, mat_table=M.table_row(lam)[None, :],
+                  force_dof=np.array([5 * centre], np.int32), force_val=np.array([1.0]),
+                  out_dof=(5 * outs).astype(np.int32), signal=st)
+    run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return [sc], run
+
+
+def random_plate(rng, edge=6.25e-3, nmin=40, nmax=80, lam=None, n_out=8, freqs=(50e3, 75e3, 100e3),
+                 dt=None, nft=None):
+    """One scenario of the batched workload (damage zones, actuator, carrier)."""
+    lam = lam or M.cfrp_laminate()
+    nex = int(rng.integers(nmin, nmax + 1))
+    ney = int(rng.integers(nmin, nmax + 1))
+    mesh = MS.structured_plate(nex * edge, ney * edge, nex, ney)
+    keep = np.ones(nex * ney)
+    for _ in range(int(rng.integers(1, 4))):
+        xc = rng.uniform(0.15, 0.85) * nex * edge
+        yc = rng.uniform(0.15, 0.85) * ney * edge
+        a = rng.uniform(5, 20) * edge / 2.5
+        b = rng.uniform(5, 20) * edge / 2.5
+        d = rng.uniform(0.2, 0.8)
+        sel = MS.elements_in_ellipse(mesh, xc, yc, a, b, rng.uniform(0, np.pi))
+        keep[sel] = 1.0 - d
+    ax_ = MS.nearest_node(mesh["coords"], rng.uniform(0.2, 0.8) * nex * edge, rng.uniform(0.2, 0.8) * ney * edge)
+    outs = MS.circle_sensor_nodes(mesh, nex * edge / 2, ney * edge / 2, 0.35 * min(nex, ney) * edge, n_out,
+                                  phase=rng.uniform(0, np.pi))
+    f = float(rng.choice(freqs))
+    sc = Scenario(mesh=mesh, mat_table=M.table_row(lam)[None, :], elem_keep=keep,
+                  force_dof=np.array([5 * ax_], np.int32), force_val=np.array([1.0]),
+                  out_dof=(5 * outs).astype(np.int32))
+    sc.carrier = f
+    return sc
+
+
+def batch(n=512, seed=0, T=0.4e-3, edge=6.25e-3, nmin=40, nmax=80, nft=None):
+    lam = M.cfrp_laminate()
+    rng = np.random.default_rng(seed)
+    dt = _dt_for(edge, edge, [lam])
+    if nft is None:
+        nft = int(np.ceil(T / dt)) + 1
+    scs = []
+    for s in range(n):
+        sc = random_plate(np.random.default_rng([seed, s]), edge, nmin, nmax, lam)
+        _, sc.signal = hanning_signal(dt, nft, sc.carrier / 5, sc.carrier, 0.0)
+        scs.append(sc)
+    run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return scs, run
+
+
+def dof_count(scenarios) -> int:
+    return int(sum(5 * np.asarray(s.mesh["coords"]).shape[0] for s in scenarios))

@@ -1,0 +1,391 @@
+"""Oracle, setup half: FP64 NumPy restatement of ma-shm's flat-shell set-up.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
+it, and only as the checker (or as the timed CPU reference arm).
+
+Every function restates one file of the reference (paths are relative to the
+ma-shm repository) in the same arithmetic order, deliberately literal: loops
+where the MATLAB code loops, the same intermediate quantities, the same
+thresholds.  The time loop itself lives in ``sem_oracle.c``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# --------------------------------------------------------------------------
+# element math
+# --------------------------------------------------------------------------
+
+
+def gll(n: int):
+    """GLL nodes and weights, ``src/models/flat_shell/flat_shell_engine/gll.m:1-39``.
+
+    gll.m hard-codes a table for n = 2..10.  The oracle recomputes the same
+    numbers from their definition (interior nodes = roots of P'_{n-1}, weights
+    2 / (n (n-1) P_{n-1}(x)^2)) with a Newton polish; the tests pin the result
+    against the table printed in gll.m (tests/golden/gll_ref.json).
+    """
+    if n == 1:
+        return np.zeros(1), np.ones(1)
+    if n == 2:
+        return np.array([-1.0, 1.0]), np.array([1.0, 1.0])
+    leg = np.polynomial.legendre.Legendre.basis(n - 1)
+    dleg = leg.deriv()
+    ddleg = dleg.deriv()
+    inner = np.sort(dleg.roots().real)
+    for _ in range(6):  # Newton polish on P'_{n-1}
+        inner = inner - dleg(inner) / ddleg(inner)
+    x = np.concatenate(([-1.0], inner, [1.0]))
+    # symmetrise exactly like the table (ksi(k) = -ksi(n+1-k))
+    x = 0.5 * (x - x[::-1])
+    w = 2.0 / (n * (n - 1) * leg(x) ** 2)
+    w = 0.5 * (w + w[::-1])
+    return x, w
+
+
+def vandermonde(ksi: np.ndarray) -> np.ndarray:
+    """``flat_shell_engine/Vandermonde.m:6-12``: V(i,j) = ksi(j)^(i-1); Q = inv(V)."""
+    n = len(ksi)
+    V = np.zeros((n, n))
+    for i in range(n):
+        for j in range(n):
+            V[i, j] = ksi[j] ** i
+    return np.linalg.inv(V)
+
+
+def shape2d_prim(nx: int, ny: int, Qx, Qy, x, y):
+    """``flat_shell_engine/shape2D_prim.m:10-58``.
+
+    Returns the element blocks Nprimx, Nprimy (nx*ny square) of the sparse
+    derivative operators Npx, Npy; node/shape numbering c = (k2-1)*nx + k1
+    (xi fastest) and entries with |v| < 1e-12 set to 0 exactly as the
+    reference does.
+    """
+    ux = np.zeros((nx, nx))
+    uy = np.zeros((ny, ny))
+    ux[:, 0] = 1.0
+    uy[:, 0] = 1.0
+    for j in range(1, nx):
+        ux[:, j] = x ** j
+    for j in range(1, ny):
+        uy[:, j] = y ** j
+    Sx = ux @ Qx.T
+    Sy = uy @ Qy.T
+    uxp = np.zeros((nx, nx))
+    uyp = np.zeros((ny, ny))
+    for j in range(1, nx):
+        uxp[:, j] = j * x ** (j - 1)
+    for j in range(1, ny):
+        uyp[:, j] = j * y ** (j - 1)
+    Sxp = uxp @ Qx.T
+    Syp = uyp @ Qy.T
+    Nx = np.zeros((nx * ny, nx * ny))
+    Ny = np.zeros((nx * ny, nx * ny))
+    c = 0
+    for k2 in range(ny):
+        for k1 in range(nx):
+            cc = 0
+            for j2 in range(ny):
+                for j1 in range(nx):
+                    vx = Sxp[k1, j1] * Sy[k2, j2]
+                    vy = Sx[k1, j1] * Syp[k2, j2]
+                    Nx[c, cc] = 0.0 if abs(vx) < 1e-12 else vx
+                    Ny[c, cc] = 0.0 if abs(vy) < 1e-12 else vy
+                    cc += 1
+            c += 1
+    return Nx, Ny
+
+
+def sparse_pattern(N: np.ndarray):
+    """MATLAB ``[i,j]=find(N)`` order (column-major), 0-based, plus values
+    (``main_flat_shell.m:267-281``)."""
+    cols, rows = np.nonzero(N.T)  # transpose => column-major enumeration
+    return rows.astype(np.int32), cols.astype(np.int32), N[rows, cols].copy()
+
+
+def jacobians(nodes1: np.ndarray, coords: np.ndarray, Nprimx, Nprimy):
+    """``main_flat_shell.m:309-350`` + ``inv_jacp_2D.m:3-8`` + ``det_jacp_2D.m:3``.
+
+    nodes1: [fen, 36] 1-based.  Returns per-local-node arrays (length
+    fen*36, element-major) J11, J21, J12, J22, invJ11, invJ12, invJ21,
+    invJ22, detJ.
+    """
+    X = coords[nodes1 - 1, 0]  # [fen,36]
+    Y = coords[nodes1 - 1, 1]
+    J11 = X @ Nprimx.T  # Npx*X, per element block
+    J21 = Y @ Nprimx.T
+    J12 = X @ Nprimy.T
+    J22 = Y @ Nprimy.T
+    a = 1.0 / (J11 * J22 - J12 * J21)
+    invJ11 = a * J22
+    invJ12 = a * (-J12)
+    invJ21 = a * (-J21)
+    invJ22 = a * J11
+    detJ = J11 * J22 - J12 * J21
+    f = lambda v: np.ascontiguousarray(v.reshape(-1))
+    return dict(J11=f(J11), J21=f(J21), J12=f(J12), J22=f(J22),
+                invJ11=f(invJ11), invJ12=f(invJ12), invJ21=f(invJ21),
+                invJ22=f(invJ22), detJ=f(detJ))
+
+
+def quad_weights(nx: int, ny: int, wx, wy):
+    """``main_flat_shell.m:400-410``: ww(cc) = wx(kx)*wy(ky), kx fastest."""
+    ww = np.zeros(nx * ny)
+    cc = 0
+    for ky in range(ny):
+        for kx in range(nx):
+            ww[cc] = wx[kx] * wy[ky]
+            cc += 1
+    return ww
+
+
+# --------------------------------------------------------------------------
+# materials
+# --------------------------------------------------------------------------
+
+
+def ply_z(lh):
+    """Ply z-ranges from the top surface downward (``lay_const.m:16-21``)."""
+    lay = len(lh)
+    h = float(np.sum(lh))
+    h2 = np.zeros(lay)
+    h1 = np.zeros(lay)
+    h2[0] = h / 2
+    h1[0] = h / 2 - lh[0]
+    for i in range(1, lay):
+        h2[i] = h2[i - 1] - lh[i - 1]
+        h1[i] = h1[i - 1] - lh[i]
+    return h, h1, h2
+
+
+def rotated_q(q11, q12, q22, q44, q55, q66, alpha_deg):
+    """Rotated ply stiffness, ``composite_plate_c_delam.m:8-20``."""
+    ar = np.asarray(alpha_deg, dtype=float) * np.pi / 180
+    m = np.cos(ar)
+    n = np.sin(ar)
+    s11 = q11 * m**4 + 2 * (q12 + 2 * q66) * m**2 * n**2 + q22 * n**4
+    s12 = (q11 + q22 - 4 * q66) * m**2 * n**2 + q12 * (m**4 + n**4)
+    s16 = (q11 - q12 - 2 * q66) * m**3 * n + (q12 - q22 + 2 * q66) * m * n**3
+    s22 = q11 * n**4 + 2 * (q12 + 2 * q66) * m**2 * n**2 + q22 * m**4
+    s26 = (q11 - q12 - 2 * q66) * n**3 * m + (q12 - q22 + 2 * q66) * n * m**3
+    s44 = q44 * m**2 + q55 * n**2
+    s45 = (q55 - q44) * m * n
+    s55 = q55 * m**2 + q44 * n**2
+    s66 = (q11 + q22 - 2 * q12) * m**2 * n**2 + q66 * (m**2 - n**2) ** 2
+    return dict(s11=s11, s12=s12, s16=s16, s22=s22, s26=s26, s44=s44,
+                s45=s45, s55=s55, s66=s66)
+
+
+ABD_KEYS = ("a11", "a12", "a16", "a22", "a26", "a66", "a44", "a45", "a55",
+            "b11", "b12", "b16", "b22", "b26", "b66",
+            "d11", "d12", "d16", "d22", "d26", "d66", "m11", "I11")
+
+
+def composite_plate_c(lh, rho, q11, q12, q22, q44, q55, q66, alpha, plies=None):
+    """Laminate ABD, shear and mass terms from ply stiffnesses.
+
+    Restates the undelaminated branch of
+    ``flat_shell_engine/composite_plate_c_delam.m:47-87`` (identical to the
+    integrals of ``composite_plate.m:52-83``).  ``plies`` restricts the sum to
+    a subset of plies (the above/below-delamination branches ``:88-173``), the
+    thickness h of the shear correction stays the full laminate's.
+    """
+    lay = len(lh)
+    h, h1, h2 = ply_z(lh)
+    rho = np.broadcast_to(np.asarray(rho, dtype=float), (lay,))
+    s = rotated_q(q11, q12, q22, q44, q55, q66, alpha)
+    s = {k: np.broadcast_to(v, (lay,)) for k, v in s.items()}
+    out = {k: 0.0 for k in ABD_KEYS}
+    for i in (range(lay) if plies is None else plies):
+        d1 = h2[i] - h1[i]
+        d2 = (h2[i] ** 2 - h1[i] ** 2) / 2
+        d3 = (h2[i] ** 3 - h1[i] ** 3) / 3
+        out["m11"] += rho[i] * (h2[i] - h1[i])
+        out["I11"] += rho[i] * (h2[i] ** 3 - h1[i] ** 3) / 3
+        shear = 5 / 4 * (h2[i] - h1[i] - 4 / 3 * (h2[i] ** 3 - h1[i] ** 3) / h**2)
+        out["a44"] += s["s44"][i] * shear
+        out["a45"] += s["s45"][i] * shear
+        out["a55"] += s["s55"][i] * shear
+        for kk in ("11", "12", "16", "22", "26", "66"):
+            out["a" + kk] += s["s" + kk][i] * d1
+            out["b" + kk] += s["s" + kk][i] * d2
+            out["d" + kk] += s["s" + kk][i] * d3
+    return out
+
+
+def add_pzt_layer(abd, h, rho_pzt, pzt_thickness, Qpzt):
+    """PZT layer on top of the laminate, ``composite_plate_c_delam_pzt.m:186-215``.
+
+    Qpzt is the 6x6 elastic matrix in the reference's (x,y,z,xz?,yz?,xy)
+    arrangement; indices below are the reference's 1-based ones minus one.
+    """
+    o = dict(abd)
+    o["m11"] += rho_pzt * pzt_thickness
+    o["I11"] += rho_pzt * ((h / 2 + pzt_thickness / 2) ** 3 - (h / 2) ** 3) / 3
+    h2_ = h / 2 + pzt_thickness / 2
+    h1_ = h / 2
+    shear = 5 / 4 * (h2_ - h1_ - 4 / 3 * (h2_**3 - h1_**3) / (h + pzt_thickness) ** 2)
+    o["a44"] += Qpzt[3, 3] * shear
+    o["a45"] += Qpzt[3, 4] * shear
+    o["a55"] += Qpzt[4, 4] * shear
+    idx = {"11": (0, 0), "12": (0, 1), "16": (0, 5), "22": (1, 1), "26": (1, 5), "66": (5, 5)}
+    for kk, (r, c) in idx.items():
+        o["a" + kk] += Qpzt[r, c] * (h2_ - h1_)
+        o["b" + kk] += Qpzt[r, c] * (h2_**2 - h1_**2) / 2
+        o["d" + kk] += Qpzt[r, c] * (h2_**3 - h1_**3) / 3
+    return o
+
+
+def pzt_const(Spzt, dp, epsT, theta_deg):
+    """``flat_shell_engine/pzt_const.m:3-37``."""
+    th = theta_deg * np.pi / 180
+    m = np.cos(th)
+    n = np.sin(th)
+    Tinv = np.array([[m**2, n**2, 0, 0, 0, -2 * m * n],
+                     [n**2, m**2, 0, 0, 0, 2 * m * n],
+                     [0, 0, 1, 0, 0, 0],
+                     [0, 0, 0, m, n, 0],
+                     [0, 0, 0, -n, m, 0],
+                     [m * n, -m * n, 0, 0, 0, m**2 - n**2]])
+    dp_ = Tinv @ np.asarray(dp).T
+    ep = dp_.T @ np.linalg.inv(Spzt)
+    gpzt = np.asarray(epsT, dtype=float)
+    Qpzt = np.linalg.inv(Spzt)
+    epzt = ep[:, [0, 1, 2, 5, 4, 3]]
+    return dict(Qpzt=Qpzt, epzt=epzt, gpzt=gpzt, e31=ep[2, 0], e32=ep[2, 1], g33=epsT[2][2])
+
+
+def engineering_2_c3d(e11, e22, e33, ni12, ni13, ni21, ni23, ni31, ni32, g12, g13, g23):
+    """``src/models/common/engineering_2_C3D.m:26-40`` (Sierakowski eq. 2.33)."""
+    Delta = (1 - ni12 * ni21 - ni13 * ni31 - ni12 * ni23 * ni31 - ni13 * ni21 * ni32 - ni23 * ni32)
+    q11 = e11 * (1 - ni23 * ni32) / Delta
+    q22 = e22 * (1 - ni31 * ni13) / Delta
+    q33 = e33 * (1 - ni12 * ni21) / Delta
+    q12 = (ni21 + ni31 * ni23) * e11 / Delta
+    q13 = (ni31 + ni21 * ni32) * e11 / Delta
+    q23 = (ni32 + ni12 * ni31) * e22 / Delta
+    return np.array([[q11, q12, q13, 0, 0, 0],
+                     [q12, q22, q23, 0, 0, 0],
+                     [q13, q23, q33, 0, 0, 0],
+                     [0, 0, 0, g23, 0, 0],
+                     [0, 0, 0, 0, g13, 0],
+                     [0, 0, 0, 0, 0, g12]])
+
+
+def c3d_2_c2d(C):
+    """``src/models/common/C3D_2_C2D.m:5-26`` (plane stress, eps_z = 0 shell)."""
+    invC = np.linalg.inv(C)
+    e11 = 1 / invC[0, 0]
+    e22 = 1 / invC[1, 1]
+    ni12 = -invC[1, 0] / invC[0, 0]
+    ni21 = -invC[0, 1] / invC[1, 1]
+    q11 = e11 / (1 - ni12 * ni21)
+    q22 = e22 / (1 - ni12 * ni21)
+    q12 = ni12 * e22 / (1 - ni12 * ni21)
+    return q11, q12, q22, C[3, 3], C[4, 4], C[5, 5]
+
+
+def damage_model(C, d):
+    """``src/models/common/damage_model.m:19-46``: C_new = C - Cd(d)."""
+    Cd11 = d * ((C[2, 2]) * (C[4, 4] / C[2, 2]) ** 2 - (C[4, 4] / C[2, 2]) ** 2)
+    Cd22 = d * ((C[2, 2]) * (C[3, 3] / C[2, 2]) ** 2 - (C[3, 3] / C[2, 2]) ** 2)
+    Cd33 = d * C[2, 2]
+    Cd44 = d * C[3, 3]
+    Cd55 = d * C[4, 4]
+    Cd66 = d * (C[2, 2] * (C[3, 3] / C[2, 2]) * (C[4, 4] / C[2, 2]) - (C[3, 3] * C[4, 4] / C[2, 2] ** 2))
+    Cd32 = d * C[2, 1]
+    Cd31 = d * C[2, 0]
+    Cd21 = (Cd22 - Cd66) / 2
+    Cd = np.array([[Cd11, Cd21, Cd31, 0, 0, 0],
+                   [Cd21, Cd22, Cd32, 0, 0, 0],
+                   [Cd31, Cd32, Cd33, 0, 0, 0],
+                   [0, 0, 0, Cd44, 0, 0],
+                   [0, 0, 0, 0, Cd55, 0],
+                   [0, 0, 0, 0, 0, Cd66]])
+    return C - Cd
+
+
+# --------------------------------------------------------------------------
+# excitation, maps, mass
+# --------------------------------------------------------------------------
+
+
+def hanning_signal(dt, nft, f_1, f_2, t_1):
+    """``flat_shell_engine/Hanning_signal.m:12-23``."""
+    t_t = 1 / f_1
+    t_2 = t_1 + t_t
+    st = np.zeros(nft)
+    t = np.zeros(nft)
+    for nf in range(nft):
+        t[nf] = nf * dt
+        if t[nf] >= t_1 and t[nf] <= t_2:
+            st[nf] = 0.5 * (1 - np.cos(2 * np.pi * f_1 * (t[nf] - t_2))) * np.sin(2 * np.pi * f_2 * (t[nf] - t_1))
+    return t, st
+
+
+def nodes_maps_fiborek(elementNodes1: np.ndarray, numberNodes: int, N: int, n_z: int = 1):
+    """12-basket conflict-free scatter maps, ``flat_shell/mesher/nodesMaps_Fiborek.m:1-27``.
+
+    elementNodes1 is 1-based [fen, npe].  Returns I_G, I_L as [rows, 12]
+    1-based arrays (0 = empty slot), rows = npe*fen/12.  The per-node
+    ``[~,S] = sort(H)`` is MATLAB's stable ascending sort.
+    """
+    n = N + 1
+    npe = n * n * n_z
+    fen = elementNodes1.shape[0]
+    Psi = np.zeros(numberNodes + 1, dtype=np.int64)
+    phi_E = np.zeros((numberNodes + 1, 12), dtype=np.int64)
+    phi_L = np.zeros((numberNodes + 1, 12), dtype=np.int64)
+    for e in range(1, fen + 1):
+        for i in range(1, npe + 1):
+            k = elementNodes1[e - 1, i - 1]
+            Psi[k] += 1
+            phi_E[k, Psi[k] - 1] = e
+            phi_L[k, Psi[k] - 1] = i
+    rows = npe * fen // 12
+    I_G = np.zeros((rows, 12), dtype=np.int64)
+    I_L = np.zeros((rows, 12), dtype=np.int64)
+    H = np.zeros(12, dtype=np.int64)
+    for k in range(1, numberNodes + 1):
+        S = np.argsort(H, kind="stable")
+        for i in range(Psi[k]):
+            H[S[i]] += 1
+            e = phi_E[k, i]
+            I_G[H[S[i]] - 1, S[i]] = k
+            I_L[H[S[i]] - 1, S[i]] = (e - 1) * npe + phi_L[k, i]
+    return I_G, I_L
+
+
+def basket_dofs(I_G, I_L, ndof_node: int = 5):
+    """``mesher/global_local_12baskets_5dofs_v2.m:32-44`` (1-based, 0 stays 0)."""
+    rows = I_G.shape[0]
+    G = np.zeros((ndof_node * rows, 12), dtype=np.int64)
+    L = np.zeros((ndof_node * rows, 12), dtype=np.int64)
+    for d in range(ndof_node):
+        G[d::ndof_node] = np.where(I_G > 0, ndof_node * I_G - (ndof_node - 1 - d), 0)
+        L[d::ndof_node] = np.where(I_L > 0, ndof_node * I_L - (ndof_node - 1 - d), 0)
+    return G, L
+
+
+def basket_scatter(F2: np.ndarray, G: np.ndarray, L: np.ndarray, ndof: int):
+    """12-basket assembly ``main_flat_shell.m:724-726`` (and mass ``:499-501``)."""
+    F = np.zeros(ndof + 1)  # slot 0 absorbs empty basket slots
+    F2p = np.concatenate(([0.0], F2))
+    for b in range(12):
+        g = G[:, b]
+        F[g] = F[g] + F2p[L[:, b]]
+    F[0] = 0.0
+    return F[1:]
+
+
+def mass_vector(WWDetJ, m11, I11, G, L, ndof):
+    """Diagonal mass ``main_flat_shell.m:493-501`` (m11/I11 scalar or per local node)."""
+    nl = WWDetJ.shape[0]
+    mgL = np.zeros(5 * nl)
+    mgL[0::5] = WWDetJ * m11
+    mgL[1::5] = WWDetJ * I11
+    mgL[2::5] = WWDetJ * m11
+    mgL[3::5] = WWDetJ * I11
+    mgL[4::5] = WWDetJ * m11
+    return basket_scatter(mgL, G, L, ndof)

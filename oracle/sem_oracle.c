@@ -1,0 +1,307 @@
+/*
+ * Oracle, time-loop half: FP64 CPU restatement of ma-shm's flat-shell
+ * explicit central-difference loop.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The product never links, loads or calls this
+ * file.  tests/ use it as the checker, bench.py's --impl reference arm and
+ * cpu_baseline leg time it as the reference's CPU path (the MATLAB original
+ * cannot run without MATLAB).
+ *
+ * It follows src/models/flat_shell/flat_shell_engine/main_flat_shell.m,
+ * MAIN LOOP (:651-920), literally, one element at a time:
+ *   gather           UX=U(Iu) ... FIY=U(Ifiy)                    :655-659
+ *   derivatives      Npx*UX ... Npy*UZ  (sparse element blocks)   :661-671
+ *   resultants       Sxx Sxxz Sxy Sxyz Syy Syyz Syz Sxz           :674-681
+ *   internal forces  fu fv mx my fw (transposed blocks)           :683-689
+ *   PZT voltage      Volt, mean over the sensor's nodes           :690-694
+ *                    (main_flat_shell_multi_pzt_c.m:619-623 for several sensors)
+ *   12-basket scatter F(I_G_dofs(:,b)) += F2(I_L_dofs(:,b))       :716-726
+ *   update           F=-F+mg2.*U+Fa*st(nn)-mg.*uold+a1*cg.*uold;
+ *                    unew=mg0.*F                                  :742-750
+ *   outputs          displ(nn,:)=U(outputs)                       :752-764
+ *   frames           v=a1*(-uold+unew) every frm_int steps        :767-776
+ *   blow-up guard    max(UZ)>10*h or isnan(unew(3))               :786-804
+ * Expression order inside each formula is the reference's (MATLAB evaluates
+ * left to right).  Element work runs in parallel with OpenMP; every basket
+ * is conflict free by construction (nodesMaps_Fiborek.m:19-27), so rows of
+ * one basket are also added in parallel with no change to the result.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NPE 36
+
+typedef struct {
+  /* mesh */
+  int32_t fen, nnode;
+  const int32_t *nodes; /* [fen*36] element-major, 1-based: nodes(ne,c) */
+  /* sparse element blocks of Npx / Npy in MATLAB find() order (0-based) */
+  int32_t nnzx, nnzy;
+  const int32_t *nx_row, *nx_col;
+  const double *nx_val;
+  const int32_t *ny_row, *ny_col;
+  const double *ny_val;
+  /* per local node (fen*36): inverse Jacobian and weights*detJ */
+  const double *invJ11, *invJ12, *invJ21, *invJ22, *WWDetJ;
+  /* per local node laminate coefficients: 21 stiffness arrays, order
+     a11 a12 a16 a22 a26 a66 a44 a45 a55 b11 b12 b16 b22 b26 b66
+     d11 d12 d16 d22 d26 d66, each fen*36 long (coef[k*L + l]) */
+  const double *coef;
+  /* basket maps I_G_dofs / I_L_dofs: [rows5 * 12] column-major, 1-based */
+  int32_t rows5;
+  const int64_t *IGd, *ILd;
+  /* diagonal matrices (already scaled as in :592-604): length 5*nnode */
+  const double *mg, *mg2, *mg0, *cg;
+  double a0, a1;
+  /* signal and loop range (1-based nn = nn_first..nft) */
+  int32_t nn_first, nft;
+  const double *st; /* [nft] */
+  /* excitation vector (dense, 5*nnode) */
+  const double *Fa;
+  /* point outputs (1-based DOF numbers) */
+  int32_t nout;
+  const int32_t *out_dof;
+  double *displ; /* [nft * nout] row-major: displ[(nn-1)*nout + k] */
+  /* PZT sensors: CSR over elements (0-based element numbers) */
+  int32_t nsens;
+  const int32_t *sens_ptr, *sens_el;
+  double pzt_thickness, g33, e31, e32, h;
+  double *voltage; /* [nft * nsens] */
+  /* frames: every frm_int steps store velocity of component frame_dof
+     (1..5) of every node into frames[c*nnode + node] */
+  int32_t frm_int, frame_dof, nframes_max;
+  double *frames;
+  double *t_frames_step; /* nn of each frame (for t_frames) */
+  int32_t nthreads;
+  /* in/out: initial and final state (5*nnode each) */
+  double *U, *uold;
+  /* result */
+  int32_t frames_written;
+  int32_t diverged_at; /* 0 if fine, else nn */
+} oracle_args;
+
+static inline void spmv_block(int nnz, const int32_t *row, const int32_t *col, const double *val,
+                              const double *x, double *y) {
+  /* y = N*x for one element block; nonzeros in column-major order */
+  for (int c = 0; c < NPE; ++c) y[c] = 0.0;
+  for (int k = 0; k < nnz; ++k) y[row[k]] += val[k] * x[col[k]];
+}
+
+static inline void spmv_block_t(int nnz, const int32_t *row, const int32_t *col, const double *val,
+                                const double *x, double *y) {
+  /* y = N'*x (N' built explicitly in the reference: Npxt=Npx') */
+  for (int c = 0; c < NPE; ++c) y[c] = 0.0;
+  for (int k = 0; k < nnz; ++k) y[col[k]] += val[k] * x[row[k]];
+}
+
+int oracle_flat_shell_run(oracle_args *A) {
+  const int fen = A->fen;
+  const int L = fen * NPE;
+  const int ndof = 5 * A->nnode;
+#ifdef _OPENMP
+  if (A->nthreads > 0) omp_set_num_threads(A->nthreads);
+#endif
+  double *F2 = (double *)calloc((size_t)5 * L, sizeof(double));
+  double *F = (double *)calloc((size_t)ndof, sizeof(double));
+  double *unew = (double *)calloc((size_t)ndof, sizeof(double));
+  double *Vsum = (double *)calloc((size_t)(fen > 0 ? fen : 1), sizeof(double));
+  if (!F2 || !F || !unew || !Vsum) return -1;
+  double *U = A->U, *uold = A->uold;
+  int frame_c = 0;
+  A->diverged_at = 0;
+  const double *cf = A->coef;
+
+  for (int nn = A->nn_first; nn <= A->nft; ++nn) {
+    double maxUZ = -INFINITY;
+#pragma omp parallel for schedule(static) reduction(max : maxUZ)
+    for (int e = 0; e < fen; ++e) {
+      double UX[NPE], UY[NPE], UZ[NPE], FIX[NPE], FIY[NPE];
+      double NpxUX[NPE], NpxUY[NPE], NpxFIX[NPE], NpxFIY[NPE];
+      double NpyUX[NPE], NpyUY[NPE], NpyFIX[NPE], NpyFIY[NPE];
+      double NpxUZ[NPE], NpyUZ[NPE];
+      double Sxx[NPE], Sxxz[NPE], Sxy[NPE], Sxyz[NPE], Syy[NPE], Syyz[NPE], Syz[NPE], Sxz[NPE];
+      double tmp[NPE], acc[NPE];
+      const int32_t *nd = A->nodes + (size_t)e * NPE;
+      for (int c = 0; c < NPE; ++c) {
+        const int g = nd[c];
+        UX[c] = U[5 * g - 5];  /* Iu   = 5*nodes-4 */
+        FIX[c] = U[5 * g - 4]; /* Ifix = 5*nodes-3 */
+        UY[c] = U[5 * g - 3];  /* Iv   = 5*nodes-2 */
+        FIY[c] = U[5 * g - 2]; /* Ifiy = 5*nodes-1 */
+        UZ[c] = U[5 * g - 1];  /* Iw   = 5*nodes   */
+        if (UZ[c] > maxUZ) maxUZ = UZ[c];
+      }
+      spmv_block(A->nnzx, A->nx_row, A->nx_col, A->nx_val, UX, NpxUX);
+      spmv_block(A->nnzx, A->nx_row, A->nx_col, A->nx_val, UY, NpxUY);
+      spmv_block(A->nnzx, A->nx_row, A->nx_col, A->nx_val, FIX, NpxFIX);
+      spmv_block(A->nnzx, A->nx_row, A->nx_col, A->nx_val, FIY, NpxFIY);
+      spmv_block(A->nnzy, A->ny_row, A->ny_col, A->ny_val, UX, NpyUX);
+      spmv_block(A->nnzy, A->ny_row, A->ny_col, A->ny_val, UY, NpyUY);
+      spmv_block(A->nnzy, A->ny_row, A->ny_col, A->ny_val, FIX, NpyFIX);
+      spmv_block(A->nnzy, A->ny_row, A->ny_col, A->ny_val, FIY, NpyFIY);
+      spmv_block(A->nnzx, A->nx_row, A->nx_col, A->nx_val, UZ, NpxUZ);
+      spmv_block(A->nnzy, A->ny_row, A->ny_col, A->ny_val, UZ, NpyUZ);
+      const size_t l0 = (size_t)e * NPE;
+      const double *iJ11 = A->invJ11 + l0, *iJ12 = A->invJ12 + l0;
+      const double *iJ21 = A->invJ21 + l0, *iJ22 = A->invJ22 + l0;
+      const double *W = A->WWDetJ + l0;
+#define C(k) (cf[(size_t)(k) * L + l0 + c])
+      for (int c = 0; c < NPE; ++c) {
+        const double a11 = C(0), a12 = C(1), a16 = C(2), a22 = C(3), a26 = C(4), a66 = C(5);
+        const double a44 = C(6), a45 = C(7), a55 = C(8);
+        const double b11 = C(9), b12 = C(10), b16 = C(11), b22 = C(12), b26 = C(13), b66 = C(14);
+        const double d11 = C(15), d12 = C(16), d16 = C(17), d22 = C(18), d26 = C(19), d66 = C(20);
+        const double i11 = iJ11[c], i12 = iJ12[c], i21 = iJ21[c], i22 = iJ22[c];
+        /* main_flat_shell.m:674-681, term by term */
+        Sxx[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * a11 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * b11 +
+                 ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * a12 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * b12 +
+                 ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * a16 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * b16 +
+                 ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * a16 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * b16;
+        Sxxz[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * b11 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * d11 +
+                  ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * b12 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * d12 +
+                  ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * b16 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * d16 +
+                  ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * b16 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * d16;
+        Sxy[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * a16 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * b16 +
+                 ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * a26 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * b26 +
+                 ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * a66 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * b66 +
+                 ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * a66 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * b66;
+        Sxyz[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * b16 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * d16 +
+                  ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * b26 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * d26 +
+                  ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * b66 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * d66 +
+                  ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * b66 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * d66;
+        Syy[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * a12 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * b12 +
+                 ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * a22 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * b22 +
+                 ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * a26 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * b26 +
+                 ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * a26 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * b26;
+        Syyz[c] = ((NpxUX[c]) * i11 + (NpyUX[c]) * i21) * b12 + ((NpxFIX[c]) * i11 + (NpyFIX[c]) * i21) * d12 +
+                  ((NpxUY[c]) * i12 + (NpyUY[c]) * i22) * b22 + ((NpxFIY[c]) * i12 + (NpyFIY[c]) * i22) * d22 +
+                  ((NpxUX[c]) * i12 + (NpyUX[c]) * i22) * b26 + ((NpxFIX[c]) * i12 + (NpyFIX[c]) * i22) * d26 +
+                  ((NpxUY[c]) * i11 + (NpyUY[c]) * i21) * b26 + ((NpxFIY[c]) * i11 + (NpyFIY[c]) * i21) * d26;
+        Syz[c] = (FIY[c] + (NpxUZ[c]) * i12 + (NpyUZ[c]) * i22) * a44 + (FIX[c] + (NpxUZ[c]) * i11 + (NpyUZ[c]) * i21) * a45;
+        Sxz[c] = (FIY[c] + (NpxUZ[c]) * i12 + (NpyUZ[c]) * i22) * a45 + (FIX[c] + (NpxUZ[c]) * i11 + (NpyUZ[c]) * i21) * a55;
+      }
+#undef C
+      /* main_flat_shell.m:683-689: each force is a left-to-right sum of
+         transposed products of weighted resultants */
+#define TERM(first, S, IJ, NPT)                                                           \
+  do {                                                                                    \
+    double v_[NPE];                                                                       \
+    for (int c = 0; c < NPE; ++c) v_[c] = S[c] * IJ[c] * W[c];                            \
+    if (NPT) spmv_block_t(A->nnzx, A->nx_row, A->nx_col, A->nx_val, v_, tmp);             \
+    else spmv_block_t(A->nnzy, A->ny_row, A->ny_col, A->ny_val, v_, tmp);                 \
+    if (first) for (int c = 0; c < NPE; ++c) acc[c] = tmp[c];                             \
+    else for (int c = 0; c < NPE; ++c) acc[c] = acc[c] + tmp[c];                          \
+  } while (0)
+      double *f2 = F2 + (size_t)5 * l0;
+      /* fu */
+      TERM(1, Sxx, iJ11, 1); TERM(0, Sxx, iJ21, 0); TERM(0, Sxy, iJ12, 1); TERM(0, Sxy, iJ22, 0);
+      for (int c = 0; c < NPE; ++c) f2[5 * c + 0] = acc[c];
+      /* fv */
+      TERM(1, Syy, iJ12, 1); TERM(0, Syy, iJ22, 0); TERM(0, Sxy, iJ11, 1); TERM(0, Sxy, iJ21, 0);
+      for (int c = 0; c < NPE; ++c) f2[5 * c + 2] = acc[c];
+      /* mx */
+      TERM(1, Sxxz, iJ11, 1); TERM(0, Sxxz, iJ21, 0); TERM(0, Sxyz, iJ12, 1); TERM(0, Sxyz, iJ22, 0);
+      for (int c = 0; c < NPE; ++c) f2[5 * c + 1] = acc[c] + Sxz[c] * W[c];
+      /* my */
+      TERM(1, Syyz, iJ12, 1); TERM(0, Syyz, iJ22, 0); TERM(0, Sxyz, iJ11, 1); TERM(0, Sxyz, iJ21, 0);
+      for (int c = 0; c < NPE; ++c) f2[5 * c + 3] = acc[c] + Syz[c] * W[c];
+      /* fw */
+      TERM(1, Syz, iJ12, 1); TERM(0, Syz, iJ22, 0); TERM(0, Sxz, iJ11, 1); TERM(0, Sxz, iJ21, 0);
+      for (int c = 0; c < NPE; ++c) f2[5 * c + 4] = acc[c];
+#undef TERM
+      /* PZT voltage partial sum (main_flat_shell.m:690-692; note invJ12 and
+         invJ21 enter the x and y derivatives here, as in the reference) */
+      if (A->nsens > 0) {
+        double s = 0.0;
+        const double k0 = A->pzt_thickness / A->g33, hh = A->h / 2;
+        for (int c = 0; c < NPE; ++c) {
+          const double v = k0 * (A->e31 * (NpxUX[c] * iJ11[c] + NpyUX[c] * iJ12[c] + hh * NpxFIX[c] * iJ11[c] +
+                                           hh * NpyFIX[c] * iJ12[c]) +
+                                 A->e32 * (NpxUY[c] * iJ21[c] + NpyUY[c] * iJ22[c] + hh * NpxFIY[c] * iJ21[c] +
+                                           hh * NpyFIY[c] * iJ22[c]));
+          s += v;
+        }
+        Vsum[e] = s;
+      }
+    }
+    /* sensor voltages: mean over all local nodes of the sensor's elements */
+    for (int k = 0; k < A->nsens; ++k) {
+      double s = 0.0;
+      int cnt = 0;
+      for (int q = A->sens_ptr[k]; q < A->sens_ptr[k + 1]; ++q) {
+        s += Vsum[A->sens_el[q]];
+        cnt += NPE;
+      }
+      A->voltage[(size_t)(nn - 1) * A->nsens + k] = cnt ? s / cnt : 0.0;
+    }
+    /* 12-basket scatter */
+    memset(F, 0, sizeof(double) * ndof);
+    for (int b = 0; b < 12; ++b) {
+      const int64_t *g = A->IGd + (size_t)b * A->rows5;
+      const int64_t *l = A->ILd + (size_t)b * A->rows5;
+#pragma omp parallel for schedule(static)
+      for (int r = 0; r < A->rows5; ++r)
+        if (g[r] > 0) F[g[r] - 1] = F[g[r] - 1] + F2[l[r] - 1];
+    }
+    /* time integration, main_flat_shell.m:742-750 */
+    const double s_nn = A->st[nn - 1];
+#pragma omp parallel for schedule(static)
+    for (int d = 0; d < ndof; ++d) {
+      double f = -F[d] + A->mg2[d] * U[d] + A->Fa[d] * s_nn - A->mg[d] * uold[d] + A->a1 * A->cg[d] * uold[d];
+      unew[d] = A->mg0[d] * f;
+    }
+    /* outputs: displacement before the update (:752-764) */
+    for (int k = 0; k < A->nout; ++k) A->displ[(size_t)(nn - 1) * A->nout + k] = U[A->out_dof[k] - 1];
+    /* frames (velocity) and blow-up guard */
+    if (A->frm_int > 0 && nn % A->frm_int == 0) {
+      if (A->frames && frame_c < A->nframes_max) {
+        double *fr = A->frames + (size_t)frame_c * A->nnode;
+        const int comp = A->frame_dof - 1;
+        for (int q = 0; q < A->nnode; ++q) fr[q] = A->a1 * (-uold[5 * q + comp] + unew[5 * q + comp]);
+        if (A->t_frames_step) A->t_frames_step[frame_c] = nn;
+        ++frame_c;
+      }
+      if (maxUZ > 10 * A->h || isnan(unew[2])) {
+        A->diverged_at = nn;
+        break;
+      }
+    }
+    /* uold = U; U = unew */
+    memcpy(uold, U, sizeof(double) * ndof);
+    memcpy(U, unew, sizeof(double) * ndof);
+  }
+  A->frames_written = frame_c;
+  free(F2);
+  free(F);
+  free(unew);
+  free(Vsum);
+  return 0;
+}
+
+/* Element force only (one application of K to U, no update): used by the
+   tests to compare element operators.  Fout = assembled K*U (5*nnode). */
+int oracle_flat_shell_apply_k(oracle_args *A, double *Fout) {
+  oracle_args B = *A;
+  /* run one "step" with mg2=mg=cg=Fa=0, mg0=-1 so that unew = F */
+  const int ndof = 5 * A->nnode;
+  double *zero = (double *)calloc((size_t)ndof, sizeof(double));
+  double *minus1 = (double *)malloc(sizeof(double) * ndof);
+  double *U = (double *)malloc(sizeof(double) * ndof);
+  double *uo = (double *)calloc((size_t)ndof, sizeof(double));
+  double st1[1] = {0.0};
+  if (!zero || !minus1 || !U || !uo) return -1;
+  for (int d = 0; d < ndof; ++d) minus1[d] = -1.0;
+  memcpy(U, A->U, sizeof(double) * ndof);
+  B.mg = zero; B.mg2 = zero; B.cg = zero; B.Fa = zero; B.mg0 = minus1;
+  B.nn_first = 1; B.nft = 1; B.st = st1; B.nout = 0; B.nsens = 0; B.frm_int = 0;
+  B.U = U; B.uold = uo;
+  int rc = oracle_flat_shell_run(&B);
+  memcpy(Fout, U, sizeof(double) * ndof);
+  free(zero); free(minus1); free(U); free(uo);
+  return rc;
+}

@@ -1,0 +1,201 @@
+"""GPU parity of the flat-shell step against the FP64 oracle, through the C ABI.
+
+Tolerances: FP64 paths <= 1e-10 relative L2 on signals and state (the only
+differences are summation order and the algebraically rearranged update);
+FP32 paths <= 1e-3 relative L2 on sensor signals (spec bound)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleProblem
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_TOL = 1e-3
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def oracle_run(sc, run, **kw):
+    orc = OracleProblem(sc.mesh["nodes"], sc.mesh["coords"], sc.mat_table, sc.elem_mat, sc.elem_keep,
+                        sc.mesh.get("I_G"), sc.mesh.get("I_L"))
+    sens = [np.asarray(s) for s in sc.sensors]
+    return orc, orc.run(run.dt, run.nft, sc.signal, nn_first=run.nn_first, eta_xy=run.eta_xy, eta_z=run.eta_z,
+                        force_dof=sc.force_dof, force_val=sc.force_val, out_dof=sc.out_dof, sensors=sens,
+                        pzt=sc.pzt, h=run.h, frm_int=run.frm_int, frame_dof=run.frame_dof, **kw)
+
+
+def small_case(pkg, nex=5, ney=4, T=4e-5, nft_cap=400, frames=0, sensors=False, keep=False):
+    scs, run = pkg.workloads.plate_force(nex=nex, ney=ney, L=0.0125 * max(nex, ney), T=T)
+    run.nft = min(run.nft, nft_cap)
+    sc = scs[0]
+    sc.signal = sc.signal[:run.nft]
+    if frames:
+        run.frm_int = frames
+    if keep:
+        sc.elem_keep = np.linspace(0.3, 1.0, nex * ney)
+    if sensors:
+        sc.sensors = [np.array([0, 1], np.int32), np.array([nex * ney - 1], np.int32)]
+        sc.pzt = dict(pzt_thickness=0.2e-3, g33=1.5e-8, e31=-5.4, e32=-5.4)
+    return scs, run
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_fp64_matches_oracle(pkg, path):
+    scs, run = small_case(pkg, frames=50, sensors=True, keep=True)
+    plan = pkg.Plan(scs, run, precision=64, path=path)
+    assert plan.info["path"] == path
+    got = plan.forward(want_frames=True)[0]
+    U, Uo = plan.get_state()
+    plan.close()
+    _, ref = oracle_run(scs[0], run)
+    assert np.abs(ref["displ"]).max() > 0
+    assert rel(got["displ"], ref["displ"]) <= FP64_TOL
+    assert rel(got["voltage"], ref["voltage"]) <= FP64_TOL
+    assert rel(got["frames"], ref["frames"]) <= FP64_TOL
+    assert rel(U, ref["U"]) <= FP64_TOL and rel(Uo, ref["uold"]) <= FP64_TOL
+
+
+def test_fp64_cfg1_full_run(pkg):
+    """Whole 0.5 ms run of the 20x20-element plate, both paths, FP64."""
+    scs, run = pkg.workloads.plate_force()
+    _, ref = oracle_run(scs[0], run)
+    for path in (1, 2):
+        plan = pkg.Plan(scs, run, precision=64, path=path, steps_per_graph=64)
+        got = plan.forward()[0]
+        plan.close()
+        assert rel(got["displ"], ref["displ"]) <= FP64_TOL, path
+
+
+def test_fp32_cfg1_within_tolerance(pkg):
+    """FP32 stepping vs the FP64 oracle on the sensor signals (displacement and
+    the derived velocity a1*(u(n+1)-u(n-1)))."""
+    scs, run = pkg.workloads.plate_force()
+    _, ref = oracle_run(scs[0], run)
+    for path in (1, 2):
+        plan = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=64)
+        got = plan.forward()[0]
+        plan.close()
+        e = rel(got["displ"], ref["displ"])
+        vg = np.diff(got["displ"][1:], axis=0)
+        vr = np.diff(ref["displ"][1:], axis=0)
+        assert e <= FP32_TOL, (path, e)
+        assert rel(vg, vr) <= FP32_TOL, path
+
+
+def test_distorted_mesh_uses_general_path(pkg):
+    from tests.test_oracle_physics import _distorted, _materials
+    mesh = _distorted(pkg, nex=4, ney=3)
+    lams = _materials(pkg)
+    table = np.stack([pkg.materials.table_row(l) for l in lams])
+    fen = mesh["nodes"].shape[0]
+    run = pkg.RunConfig(dt=5e-9, nft=300, nn_first=1, eta_xy=4e2, eta_z=4e3, h=3.9e-3)
+    _, st = pkg.hanning_signal(run.dt, run.nft, 100e3, 500e3)
+    centre = pkg.mesh.nearest_node(mesh["coords"], 0.02, 0.01)
+    sc = pkg.Scenario(mesh=mesh, mat_table=table, elem_mat=np.arange(fen) % 2,
+                      elem_keep=np.linspace(0.5, 1, fen), force_dof=np.array([5 * centre, 5 * centre - 4]),
+                      force_val=np.array([1.0, 0.3]), out_dof=np.arange(1, 5 * mesh["coords"].shape[0], 37),
+                      signal=st, sensors=[np.array([2, 3], np.int32)],
+                      pzt=dict(pzt_thickness=0.2e-3, g33=1.5e-8, e31=-5.4, e32=-4.0))
+    plan = pkg.Plan([sc], run, precision=64, path=0)
+    assert plan.info["path"] == 1   # jittered quads: structured kernel refuses
+    got = plan.forward()[0]
+    plan.close()
+    _, ref = oracle_run(sc, run)
+    assert rel(got["displ"], ref["displ"]) <= FP64_TOL
+    assert rel(got["voltage"], ref["voltage"]) <= FP64_TOL
+
+
+def test_apply_stiffness_matches_oracle(pkg):
+    from tests.test_oracle_physics import _distorted, _materials
+    mesh = _distorted(pkg, nex=4, ney=3)
+    lams = _materials(pkg)
+    table = np.stack([pkg.materials.table_row(l) for l in lams])
+    fen = mesh["nodes"].shape[0]
+    em, keep = np.arange(fen) % 2, np.linspace(0.5, 1, fen)
+    sc = pkg.Scenario(mesh=mesh, mat_table=table, elem_mat=em, elem_keep=keep, signal=np.zeros(4))
+    run = pkg.RunConfig(dt=1e-8, nft=4)
+    U = np.random.default_rng(0).standard_normal(5 * mesh["coords"].shape[0]) * 1e-9
+    orc = OracleProblem(mesh["nodes"], mesh["coords"], table, em, keep)
+    Fo = orc.apply_k(U)
+    for prec, tol in ((64, 1e-12), (32, 2e-5)):
+        plan = pkg.Plan([sc], run, precision=prec)
+        F = plan.apply_stiffness(U)
+        np.testing.assert_allclose(plan.mass(), orc.mg_raw, rtol=1e-13)
+        plan.close()
+        assert rel(F, Fo) <= tol, prec
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_batch_equals_solo(pkg, path):
+    """Scenarios of uneven size in one plan give the same bits as solo runs."""
+    rng = np.random.default_rng(5)
+    scs = []
+    for s in range(3):
+        sc = pkg.workloads.random_plate(np.random.default_rng([1, s]), edge=6.25e-3, nmin=3, nmax=7)
+        scs.append(sc)
+    dt = 1.0e-7
+    nft = 250
+    for sc in scs:
+        _, sc.signal = pkg.hanning_signal(dt, nft, sc.carrier / 5, sc.carrier)
+    run = pkg.RunConfig(dt=dt, nft=nft, eta_xy=4e2, eta_z=4e3, h=3.9e-3)
+    for prec in (64, 32):
+        plan = pkg.Plan(scs, run, precision=prec, path=path, steps_per_graph=32)
+        batch = plan.forward()
+        plan.close()
+        for s, sc in enumerate(scs):
+            p1 = pkg.Plan([sc], run, precision=prec, path=path)
+            solo = p1.forward()[0]
+            p1.close()
+            np.testing.assert_array_equal(batch[s]["displ"], solo["displ"])
+    del rng
+
+
+def test_graph_and_resume_are_bit_identical(pkg):
+    scs, run = small_case(pkg, nft_cap=300)
+    for path in (1, 2):
+        a = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=0)
+        ra = a.forward()[0]
+        b = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=37)
+        rb = b.forward()[0]
+        np.testing.assert_array_equal(ra["displ"], rb["displ"])
+        # checkpoint at step 150, resume in a fresh plan
+        b.reset()
+        b.set_signal()
+        b.advance(150 - run.nn_first)
+        U, Uo = b.get_state()
+        c = pkg.Plan(scs, run, precision=32, path=path)
+        c.set_signal()
+        c.set_state(U, Uo, 150)
+        c.advance(run.nft - 150 + 1)
+        Uc, _ = c.get_state()
+        Ua, _ = a.get_state()
+        np.testing.assert_array_equal(Uc, Ua)
+        for p in (a, b, c):
+            p.close()
+
+
+def test_divergence_is_reported(pkg):
+    """dt far above the stability limit: the blow-up guard returns
+    SHM_ERR_DIVERGED (non-finite arithmetic only, no device fault)."""
+    scs, run = small_case(pkg, nft_cap=400, frames=20)
+    run.dt *= 6
+    plan = pkg.Plan(scs, run, precision=32, path=0)
+    with pytest.raises(pkg.native.ShmError) as ei:
+        plan.forward()
+    assert ei.value.status == pkg.native.SHM_ERR_DIVERGED
+    plan.close()
+
+
+def test_invalid_inputs_rejected(pkg):
+    scs, run = small_case(pkg)
+    sc = scs[0]
+    bad = pkg.Scenario(mesh=sc.mesh, mat_table=sc.mat_table, force_dof=np.array([10 ** 9], np.int32),
+                       force_val=np.array([1.0]), signal=sc.signal)
+    with pytest.raises(pkg.native.ShmError) as ei:
+        pkg.Plan([bad], run)
+    assert ei.value.status == pkg.native.SHM_ERR_BAD_ARG
+    with pytest.raises(pkg.native.ShmError):
+        pkg.Plan(scs, run, path=2, precision=16)
