@@ -120,10 +120,12 @@ def test_apply_stiffness_matches_oracle(pkg):
     U = np.random.default_rng(0).standard_normal(5 * mesh["coords"].shape[0]) * 1e-9
     orc = OracleProblem(mesh["nodes"], mesh["coords"], table, em, keep)
     Fo = orc.apply_k(U)
-    for prec, tol in ((64, 1e-12), (32, 2e-5)):
+    # the product's Jacobians come from its own D matrix (barycentric), the
+    # oracle's from the reference's inverse Vandermonde: ~1e-13 apart
+    for prec, tol in ((64, 1e-11), (32, 2e-5)):
         plan = pkg.Plan([sc], run, precision=prec)
         F = plan.apply_stiffness(U)
-        np.testing.assert_allclose(plan.mass(), orc.mg_raw, rtol=1e-13)
+        np.testing.assert_allclose(plan.mass(), orc.mg_raw, rtol=1e-12)
         plan.close()
         assert rel(F, Fo) <= tol, prec
 
