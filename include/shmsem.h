@@ -140,6 +140,29 @@ shm_status shm_plan_info(const shm_plan *plan, int64_t *info8);
  * [total_nodes x 5] interleaved. */
 shm_status shm_mass(shm_plan *plan, double *mg);
 
+/* Allocation-free internal force.  No counterpart in the reference: it is the
+ * element step (gather, K_e*u_e) plus the reference's 12-basket assembly,
+ * exposed for callers that must not allocate device memory -- a MEX gateway
+ * whose gpuArray memory belongs to MATLAB's GPU memory manager, or a
+ * long-running monitoring loop on a fixed memory budget.  Every pointer is a
+ * DEVICE pointer owned by the caller:
+ *   nodes  [fen x 36] column-major, 1-based (mesh `nodes`)
+ *   coords [nnode x 3] column-major (mesh `coords`, z unused)
+ *   lam    [21 x fen]: coefficient q of element e at lam[q*fen + e], order
+ *          a11 a12 a16 a22 a26 a66 a44 a45 a55 b11 b12 b16 b22 b26 b66 d11 d12 d16 d22 d26 d66
+ *   I_G, I_L [basket_rows x 12] column-major, 1-based, 0 = empty (nodesMaps_Fiborek.m)
+ *   U, F   [5*nnode] in the reference DOF order (u, phi_x, v, phi_y, w per node)
+ * The element-local forces live in a fixed device array inside the library
+ * (SHM_STATIC_MAX_ELEMS elements, 5.9 MB, held by every GPU that loads the
+ * library until exit); larger meshes return SHM_ERR_BAD_ARG.  The first call
+ * on a device sets up that device (symbol address, constants): make it before
+ * any stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race; calls ordered on one stream are safe.  FP64. */
+#define SHM_STATIC_MAX_ELEMS 4096
+shm_status shm_stiffness_static(int32_t fen, int32_t nnode, const int32_t *nodes, const double *coords,
+                                const double *lam, int32_t basket_rows, const int32_t *I_G, const int32_t *I_L,
+                                const double *U, double *F, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,7 +13,7 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libshmsem.so")
-SOURCES = [os.path.join(PKG_DIR, "csrc", "shmsem.cu")]
+SOURCES = [os.path.join(PKG_DIR, "csrc", f) for f in ("shmsem.cu", "static_stiffness.cu")]
 HEADERS = [os.path.join(PKG_DIR, "csrc", f) for f in ("shell_element.cuh", "shell_structured.cuh")] + [
     os.path.join(REPO_DIR, "include", "shmsem.h")]
 

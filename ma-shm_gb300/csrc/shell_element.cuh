@@ -31,11 +31,13 @@ constexpr int ELEM_STRIDE = 181; // odd shared-memory stride per element (>= 5*3
 constexpr int CTA_ELEMS = 32;    // elements per CTA (one per lane)
 constexpr int CTA_THREADS = 192; // 6 warps
 
-// GLL derivative matrix D[r][c] = l_c'(x_r) and weights, filled at plan set-up.
-__constant__ double c_D64[NP * NP];
-__constant__ float c_D32[NP * NP];
-__constant__ double c_w64[NP];
-__constant__ float c_w32[NP];
+// GLL derivative matrix D[r][c] = l_c'(x_r) and weights, filled at set-up.
+// Internal linkage: every translation unit that includes this header owns
+// (and initialises) its own copy.
+static __constant__ double c_D64[NP * NP];
+static __constant__ float c_D32[NP * NP];
+static __constant__ double c_w64[NP];
+static __constant__ float c_w32[NP];
 
 template <typename T> __device__ __forceinline__ T Dm(int r, int c);
 template <> __device__ __forceinline__ double Dm<double>(int r, int c) { return c_D64[r * NP + c]; }
