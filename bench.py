@@ -156,6 +156,8 @@ def main():
     ap.add_argument("--precision", type=int, default=32)
     ap.add_argument("--graph", type=int, default=50)
     ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--rows", type=int, default=0)
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -193,7 +195,13 @@ def main():
 
     import torch
     plan = pkg.Plan(scs, run, precision=args.precision, path=0, steps_per_graph=args.graph,
-                    tile_elems=args.tile, device=local)
+                    tile_elems=args.tile, device=local, rows_per_block=args.rows)
+    tuned = None
+    if plan.info["path"] == 2 and args.tile == 0 and args.rows == 0 and not args.no_tune:
+        tuned = plan.autotune(10)
+    config["tile_elems"] = plan.info["tile"]
+    config["rows_per_block"] = plan.info["rows_per_block"]
+    config["autotuned"] = tuned is not None
     plan.reset()
     plan.set_signal()
     nmax = run.nft - run.nn_first + 1

@@ -91,10 +91,12 @@ typedef struct {
 
 typedef struct {
   int32_t precision;       /* 64 or 32 (state and element arithmetic) */
-  int32_t path;            /* 0 auto, 1 general (element + node kernels), 2 structured fused */
+  int32_t path;            /* 0 auto, 1 general (element + node kernels), 2 structured fused,
+                              3 structured fused with the generic (unpacked) FP32 kernel */
   int32_t steps_per_graph; /* CUDA-graph chunk length, 0 = plain launches */
-  int32_t tile_elems;      /* structured path: elements per warp line (16/32), 0 = autotune */
+  int32_t tile_elems;      /* structured path: elements per lane group (16/32), 0 = by lane use */
   int32_t device;          /* CUDA device ordinal */
+  int32_t rows_per_block;  /* structured path: element rows per task, 0 = 16 */
 } shm_options;
 
 /* Creates a plan for `nscen` scenarios advanced together (one launch per
@@ -133,8 +135,15 @@ shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
 
 /* Plan facts: [0] total nodes, [1] total elements, [2] total DOF, [3] path
  * used (1 general, 2 structured), [4] precision, [5] frames per scenario,
- * [6] kernel launches per step, [7] tile elements (structured). */
-shm_status shm_plan_info(const shm_plan *plan, int64_t *info8);
+ * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task. */
+shm_status shm_plan_info(const shm_plan *plan, int64_t *info9);
+
+/* Autotuner of the structured kernel: times `steps` steps for every
+ * (elements per lane group, element rows per task) candidate -- {16, 32} x
+ * {4, 8, 16, 32, 64} -- re-planning the task list each time, keeps the
+ * fastest and resets the state.  Returns the choice and its ms per step. */
+shm_status shm_autotune(shm_plan *plan, int32_t steps, int32_t *tile_elems, int32_t *rows_per_block,
+                        float *ms_per_step);
 
 /* Diagonal mass vector of the plan (reference mg before scaling, :493-501),
  * [total_nodes x 5] interleaved. */

@@ -1,0 +1,503 @@
+// Structured fused flat-shell step, FP32 specialisation for sm_103a.
+//
+// Same decomposition as k_struct_step (shell_structured.cuh: strips of EW-1
+// element columns swept bottom to top, shared-memory force band, every node
+// owned by one task), restructured for throughput:
+//  * u_n of the strip lives in a shared-memory ring of 11 node rows; the 5 new
+//    node rows of the next element row are copied with cp.async while the
+//    current row is computed, so the gather never waits on memory;
+//  * the 6x6 contractions, resultants and fluxes run on packed FP32x2 FMA
+//    (__ffma2_rn, two lanes of a 64-bit register pair per instruction);
+//  * the force band is a 6-row ring (the shared node row is carried by
+//    re-labelling, not copied);
+//  * the update's loads of u_{n-1} and 1/M are issued before phase C so that
+//    their latency overlaps the transposed operator.
+// Results equal the generic kernel's up to FP32 rounding order.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "shell_element.cuh"
+#include "shell_structured.cuh"
+
+namespace shm {
+
+// c_Dp[k][p]  = (D[2p][k], D[2p+1][k])   for out[i]  += D[i][k] * in[k]
+// c_DTp[k][p] = (D[k][2p], D[k][2p+1])   for out[m]  += D[k][m] * in[k]
+static __constant__ float2 c_Dp[NP][3];
+static __constant__ float2 c_DTp[NP][3];
+
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+// laminate coefficient pairs, in the order the resultant pairs use them
+// (Nxx,Nyy): (a11,a12) (a12,a22) (a16,a26) (b11,b12) (b12,b22) (b16,b26)
+// (Nxy,Mxx): (a16,b11) (a26,b12) (a66,b16) (b16,d11) (b26,d12) (b66,d16)
+// (Myy,Mxy): (b12,b16) (b22,b26) (b26,b66) (d12,d16) (d22,d26) (d26,d66)
+// (Qy,Qx):   (a44,a45) (a45,a55)
+constexpr int LAMP = 20;
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int EW> struct F32Geom {
+  static constexpr int G = 32 / EW;
+  static constexpr int W = 5 * EW + 1;          // band columns
+  static constexpr int OWN = 5 * (EW - 1);      // owned columns
+  static constexpr int URING = 11;              // u_n node rows kept
+  static constexpr int URAW = URING * 5 * W;
+  static constexpr int UGS = URAW + ((16 - URAW % 32) + 64) % 32;   // group stride = 16 mod 32
+  static constexpr int FRAW = 6 * 5 * W;
+  static constexpr int FGS = FRAW + ((16 - FRAW % 32) + 64) % 32;
+  static constexpr int NUPD = (G * 6 * OWN + CTA_THREADS - 1) / CTA_THREADS;  // update nodes per thread
+};
+
+template <int EW>
+constexpr size_t struct_f32_smem_bytes() {
+  using GM = F32Geom<EW>;
+  return sizeof(float) * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS + GM::G * (GM::UGS + GM::FGS));
+}
+
+struct F32Args {
+  const PlateDesc* __restrict__ plates;
+  const TaskDesc* __restrict__ tasks;
+  int ntask, H, nn_first, nft;
+  int64_t nnode_pad;
+  float* UA;
+  float* UB;
+  const float* __restrict__ minv;
+  float k1[5], k2[5];
+  const float2* __restrict__ matp;  // [nmat][20] coefficient pairs
+  const int* __restrict__ emat_g;
+  const float* __restrict__ ekeep_g;
+  const int* __restrict__ esens_g;
+  const int* __restrict__ f_xl;
+  const int* __restrict__ f_iy;
+  const int* __restrict__ f_field;
+  const double* __restrict__ f_val;
+  const double* __restrict__ st;
+  int nout;
+  const int* __restrict__ out_node;
+  const int* __restrict__ out_field;
+  double* displ;
+  double* vsum;
+  SensorConst<float> sc;
+  int frm_int, frame_field, nframes;
+  float* frames;
+  float a1, blowup;
+  int* flag;
+  const int* d_base;
+};
+
+// per-group task facts, uniform inside the group
+struct GroupTask {
+  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, scen;
+  long long node0, egrid0;
+  float sx, sy, area4;
+};
+
+__device__ __forceinline__ GroupTask load_group_task(const F32Args& a, int tid) {
+  GroupTask t{};
+  if (tid >= a.ntask) return t;
+  const TaskDesc tk = a.tasks[tid];
+  const PlateDesc pl = a.plates[tk.plate];
+  t.has = 1;
+  t.nrows = tk.nrows;
+  t.block = tk.block;
+  t.eyA = tk.block == 0 ? 0 : tk.block * a.H - 1;
+  t.strip = tk.strip;
+  t.plate = tk.plate;
+  t.ney = pl.ney;
+  t.nex = pl.nex;
+  t.NX = pl.NX;
+  t.f0 = tk.f0;
+  t.fn = tk.fn;
+  t.scen = pl.scen;
+  t.node0 = pl.node0;
+  t.egrid0 = pl.egrid0;
+  t.sx = (float)pl.sx;
+  t.sy = (float)pl.sy;
+  t.area4 = (float)pl.area4;
+  return t;
+}
+
+template <int G>
+__device__ __forceinline__ const GroupTask& pick(const GroupTask* gt, int g) {
+  if constexpr (G == 1) {
+    return gt[0];
+  } else {
+    return gt[g];
+  }
+}
+
+// copy node rows [r0, r0+nr) (relative to the task's first node row) of u_n
+// into the ring; columns outside the plate are left untouched (never read)
+template <int EW>
+__device__ __forceinline__ void ring_load(float* ring, const float* __restrict__ cur, int64_t nnode_pad,
+                                          const GroupTask* gt, int r0, int nr) {
+  using GM = F32Geom<EW>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per_group = nr * 5;
+  for (int rf = warp; rf < GM::G * per_group; rf += CTA_THREADS / 32) {
+    const int gg = rf / per_group;
+    const int rem = rf % per_group;
+    const int rr = rem / 5, f = rem % 5;
+    const GroupTask& t = pick<GM::G>(gt, gg);
+    if (!t.has) continue;
+    const int row = 5 * t.eyA + r0 + rr;
+    if (row > 5 * t.ney) continue;
+    const int col0 = 5 * (t.strip * (EW - 1) - 1);
+    float* dst = ring + gg * GM::UGS + (((r0 + rr) % GM::URING) * 5 + f) * GM::W;
+    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row * t.NX + col0;
+    for (int c = lane; c < GM::W; c += 32) {
+      const int col = col0 + c;
+      if (col >= 0 && col < t.NX) cp_async4(dst + c, src + c);
+    }
+  }
+}
+
+template <int EW, bool kSensor>
+__global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, int kstep) {
+  using GM = F32Geom<EW>;
+  constexpr int G = GM::G;
+  constexpr int W = GM::W;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* sm = reinterpret_cast<float*>(smraw);
+  float* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
+  float* ring = vred + NP * CTA_ELEMS;
+  float* band = ring + G * GM::UGS;
+
+  const int nn = *a.d_base + kstep;
+  const bool odd = ((nn - a.nn_first) & 1);
+  const float* __restrict__ cur = odd ? a.UB : a.UA;
+  float* prev = odd ? a.UA : a.UB;
+  if (blockIdx.x == 0)
+    for (int q = threadIdx.x; q < a.nout; q += blockDim.x)
+      a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
+
+  const int j = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / EW;
+  const int q = lane % EW;
+  float* xs = sm + lane * ELEM_STRIDE;
+  float* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
+  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  const int ntg = (a.ntask + G - 1) / G;
+  bool bad = false;
+  // owned band entries this thread updates: (group, logical row, owned column)
+  int ent_g[GM::NUPD], ent_r[GM::NUPD], ent_c[GM::NUPD];
+#pragma unroll
+  for (int s = 0; s < GM::NUPD; ++s) {
+    const int idx = threadIdx.x + s * CTA_THREADS;
+    const bool ok = idx < G * 6 * GM::OWN;
+    ent_g[s] = ok ? idx / (6 * GM::OWN) : 0;
+    const int rem = idx % (6 * GM::OWN);
+    ent_r[s] = rem / GM::OWN;
+    ent_c[s] = ok ? rem % GM::OWN : -1;
+  }
+  float uo_r[GM::NUPD][5];
+  float mt_r[GM::NUPD], mr_r[GM::NUPD];
+  int64_t node_r[GM::NUPD];
+
+  __shared__ GroupTask gt[G];  // task facts of the lane groups (shared, not in registers)
+  for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < G) gt[threadIdx.x] = load_group_task(a, tg * G + threadIdx.x);
+    __syncthreads();
+    int maxrows = 0;
+#pragma unroll
+    for (int gg = 0; gg < G; ++gg) maxrows = max(maxrows, gt[gg].nrows);
+    const GroupTask& t = pick<G>(gt, g);
+    const int ex = t.strip * (EW - 1) - 1 + q;
+    float* ub = ring + g * GM::UGS;
+    float* fb = band + g * GM::FGS;
+    const float2 wsxy = make_float2(t.sx, t.sy);
+
+    for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
+    ring_load<EW>(ring, cur, a.nnode_pad, gt, 0, 6);
+    cp_async_commit();
+
+    for (int r = 0; r < maxrows; ++r) {
+      // next element row's five new node rows (ring slots free since row r-1)
+      if (r + 1 < maxrows) ring_load<EW>(ring, cur, a.nnode_pad, gt, 5 * r + 6, 5);
+      cp_async_commit();
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      __syncthreads();
+
+      const int ey = t.eyA + r;
+      const bool rowact = r < t.nrows;
+      const bool valid = rowact && ex >= 0 && ex < t.nex;
+      const int64_t egrid = t.egrid0 + (int64_t)ey * t.nex + ex;
+      const int s0 = 5 * r;  // first node row of this element row (task-relative)
+
+      // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
+      if (valid) {
+        const float* urow = ub + ((s0 + j) % GM::URING) * 5 * W + 5 * q;
+        float2 acc[5][3];
+#pragma unroll
+        for (int f = 0; f < 5; ++f)
+#pragma unroll
+          for (int p = 0; p < 3; ++p) acc[f][p] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            const float2 u2 = bc2(urow[f * W + k]);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) acc[f][p] = fma2(c_Dp[k][p], u2, acc[f][p]);
+          }
+        const float2 sx2 = bc2(t.sx);
+#pragma unroll
+        for (int f = 0; f < 5; ++f)
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            const float2 d = mul2(acc[f][p], sx2);
+            ys[f * NPE + (2 * p) * NP + j] = d.x;
+            ys[f * NPE + (2 * p + 1) * NP + j] = d.y;
+          }
+      }
+      __syncthreads();
+      // phase B: column i = j
+      if (valid) {
+        const int i = j;
+        float v[5][NP];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+          const float* urow = ub + ((s0 + k) % GM::URING) * 5 * W + 5 * q + i;
+#pragma unroll
+          for (int f = 0; f < 5; ++f) v[f][k] = urow[f * W];
+        }
+        // eta-derivatives, packed over node pairs, scaled by 2/ay
+        float2 de2[5][3];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) de2[f][p] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int m = 0; m < NP; ++m) {
+            const float2 v2 = bc2(v[f][m]);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) de2[f][p] = fma2(c_Dp[m][p], v2, de2[f][p]);
+          }
+#pragma unroll
+          for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t.sy));
+        }
+        float2 L[LAMP];
+        {
+          const float2* mp = a.matp + (int64_t)a.emat_g[egrid] * LAMP;
+          const float2 kp = bc2(a.ekeep_g[egrid]);
+#pragma unroll
+          for (int c = 0; c < LAMP; ++c) L[c] = mul2(mp[c], kp);
+        }
+        float2 Fe2[5][3];
+#pragma unroll
+        for (int f = 0; f < 5; ++f)
+#pragma unroll
+          for (int p = 0; p < 3; ++p) Fe2[f][p] = make_float2(0.f, 0.f);
+        float vp = 0.f;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+          float gx[5], gy[5];
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            gx[f] = ys[f * NPE + i * NP + k];
+            gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
+          }
+          const float ex_ = gx[0], ey_ = gy[2], gxy = gy[0] + gx[2];
+          const float kx = gx[1], ky = gy[3], kxy = gy[1] + gx[3];
+          const float gyz = v[3][k] + gy[4];
+          const float gxz = v[1][k] + gx[4];
+          float2 NN = mul2(L[0], bc2(ex_));
+          NN = fma2(L[1], bc2(ey_), NN);
+          NN = fma2(L[2], bc2(gxy), NN);
+          NN = fma2(L[3], bc2(kx), NN);
+          NN = fma2(L[4], bc2(ky), NN);
+          NN = fma2(L[5], bc2(kxy), NN);          // (Nxx, Nyy)
+          float2 NM = mul2(L[6], bc2(ex_));
+          NM = fma2(L[7], bc2(ey_), NM);
+          NM = fma2(L[8], bc2(gxy), NM);
+          NM = fma2(L[9], bc2(kx), NM);
+          NM = fma2(L[10], bc2(ky), NM);
+          NM = fma2(L[11], bc2(kxy), NM);         // (Nxy, Mxx)
+          float2 MM = mul2(L[12], bc2(ex_));
+          MM = fma2(L[13], bc2(ey_), MM);
+          MM = fma2(L[14], bc2(gxy), MM);
+          MM = fma2(L[15], bc2(kx), MM);
+          MM = fma2(L[16], bc2(ky), MM);
+          MM = fma2(L[17], bc2(kxy), MM);         // (Myy, Mxy)
+          float2 QQ = mul2(L[18], bc2(gyz));
+          QQ = fma2(L[19], bc2(gxz), QQ);         // (Qy, Qx)
+          const float Wn = c_w32[i] * c_w32[k] * t.area4;
+          const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
+          // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
+          const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
+          const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
+          const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
+          const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
+          const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
+          const float2 Gs[5] = {G0, G1, G2, G3, G4};
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            ys[f * NPE + i * NP + k] = Gs[f].x;
+            const float2 ge = bc2(Gs[f].y);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
+          }
+          if (k & 1) {
+            Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
+            Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
+          } else {
+            Fe2[1][k >> 1].x += Wn * QQ.y;
+            Fe2[3][k >> 1].x += Wn * QQ.x;
+          }
+          if (kSensor) {
+            vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
+          }
+        }
+#pragma unroll
+        for (int f = 0; f < 5; ++f)
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            xs[f * NPE + i * NP + 2 * p] = Fe2[f][p].x;
+            xs[f * NPE + i * NP + 2 * p + 1] = Fe2[f][p].y;
+          }
+        if (kSensor) vred[i * CTA_ELEMS + lane] = vp;
+      }
+      __syncthreads();
+
+      // the update's global loads for this element row, issued before phase C
+#pragma unroll
+      for (int s = 0; s < GM::NUPD; ++s) {
+        node_r[s] = -1;
+        if (ent_c[s] < 0) continue;
+        const GroupTask& t2 = pick<G>(gt, ent_g[s]);
+        const int rr = ent_r[s];
+        if (!t2.has || r >= t2.nrows || (t2.block > 0 && r == 0)) continue;
+        const int ey2 = t2.eyA + r;
+        if (rr >= ((ey2 == t2.ney - 1) ? 6 : 5)) continue;
+        const int ix = 5 * t2.strip * (EW - 1) + ent_c[s];
+        if (ix >= t2.NX) continue;
+        const int64_t node = t2.node0 + (int64_t)(5 * ey2 + rr) * t2.NX + ix;
+        node_r[s] = node;
+        mt_r[s] = a.minv[node];
+        mr_r[s] = a.minv[a.nnode_pad + node];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) uo_r[s][f] = prev[f * a.nnode_pad + node];
+      }
+
+      // phase C: xi-part of the transposed operator + column part
+      float out[5][NP];
+      if (valid) {
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+          float2 o2[3];
+#pragma unroll
+          for (int p = 0; p < 3; ++p) o2[p] = make_float2(xs[f * NPE + (2 * p) * NP + j], xs[f * NPE + (2 * p + 1) * NP + j]);
+#pragma unroll
+          for (int ii = 0; ii < NP; ++ii) {
+            const float2 gg2 = bc2(ys[f * NPE + ii * NP + j]);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) o2[p] = fma2(c_DTp[ii][p], gg2, o2[p]);
+          }
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            out[f][2 * p] = o2[p].x;
+            out[f][2 * p + 1] = o2[p].y;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < 5; ++f)
+#pragma unroll
+          for (int i = 0; i < NP; ++i) out[f][i] = 0.f;
+      }
+      // band accumulation.  Logical row j of this element row is physical row
+      // (j - r) mod 6.  Row 0 carries the previous element row's top line and
+      // is added to; rows 1..5 start here, so pass 1 stores columns i = 0..4
+      // (lanes without an element store zeros) and pass 2 adds column i = 5
+      // (the next lane's column 0), or stores it on the strip's last lane.
+      {
+        float* dst = fb + ((j - r % 6 + 6) % 6) * 5 * W + 5 * q;
+        if (j == 0) {
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int i = 0; i < 5; ++i) dst[f * W + i] += out[f][i];
+        } else {
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int i = 0; i < 5; ++i) dst[f * W + i] = out[f][i];
+        }
+        __syncthreads();
+        if (j == 0 || q < EW - 1) {
+#pragma unroll
+          for (int f = 0; f < 5; ++f) dst[f * W + 5] += out[f][5];
+        } else {
+#pragma unroll
+          for (int f = 0; f < 5; ++f) dst[f * W + 5] = out[f][5];
+        }
+        __syncthreads();
+      }
+      const bool owned_row = rowact && (t.block == 0 || r > 0);
+      if (kSensor && j == 0 && valid && owned_row && q > 0) {
+        const int slot = a.esens_g[egrid];
+        if (slot >= 0) {
+          double s = 0.0;
+#pragma unroll
+          for (int i = 0; i < NP; ++i) s += (double)vred[i * CTA_ELEMS + lane];
+          a.vsum[(int64_t)slot * a.nft + (nn - 1)] = s;
+        }
+      }
+      // update owned, complete nodes (excitation added here by the node's owner)
+#pragma unroll
+      for (int s = 0; s < GM::NUPD; ++s) {
+        if (node_r[s] < 0) continue;
+        const int gg = ent_g[s], rr = ent_r[s], c = ent_c[s];
+        const GroupTask& t2 = pick<G>(gt, gg);
+        const float* bnd = band + gg * GM::FGS + ((rr - r % 6 + 6) % 6) * 5 * W + 5 + c;
+        const float* urow = ring + gg * GM::UGS + ((5 * r + rr) % GM::URING) * 5 * W + 5 + c;
+        const int64_t node = node_r[s];
+        float F[5];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) F[f] = bnd[f * W];
+        if (t2.fn > 0) {
+          const int iy = 5 * (t2.eyA + r) + rr;
+          for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)
+            if (a.f_iy[fi] == iy && a.f_xl[fi] == 5 + c) {
+              const float fs = (float)(a.f_val[fi] * a.st[(int64_t)t2.scen * a.nft + (nn - 1)]);
+#pragma unroll
+              for (int f = 0; f < 5; ++f)
+                if (f == a.f_field[fi]) F[f] -= fs;
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+          const float u = urow[f * W];
+          const float uo = uo_r[s][f];
+          const float im = (f == 1 || f == 3) ? mr_r[s] : mt_r[s];
+          const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
+          prev[f * a.nnode_pad + node] = un;
+          if (frame) {
+            if (f == a.frame_field) {
+              const int fc = nn / a.frm_int - 1;
+              if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + node] = a.a1 * (un - uo);
+            }
+            if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
+          }
+        }
+      }
+      // ring slots read above are refilled by the next row's prefetch
+      __syncthreads();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  if (bad) atomicOr(a.flag, 1);
+}
+
+}  // namespace shm

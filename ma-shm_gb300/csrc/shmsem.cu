@@ -225,6 +225,12 @@ __global__ void k_voltage(const double* vsum, const int* sptr, double* volt, int
 // structured fused path (declared here, defined in shell_structured.cuh)
 // ---------------------------------------------------------------------------
 #include "shell_structured.cuh"
+#include "shell_structured_f32.cuh"
+
+// laminate coefficient pairs for the packed FP32 kernel (indices into a table row)
+static const int kLamPairs[LAMP][2] = {{0, 1},   {1, 3},   {2, 4},   {9, 10},  {10, 12}, {11, 13}, {2, 9},
+                                       {4, 10},  {5, 11},  {11, 15}, {13, 16}, {14, 17}, {10, 11}, {12, 13},
+                                       {13, 14}, {16, 17}, {18, 19}, {19, 20}, {6, 7},   {7, 8}};
 
 struct StructPlan {
   int tile = 32, H = 16, ntask = 0, grid = 0;
@@ -235,6 +241,12 @@ struct StructPlan {
   int* esens_g = nullptr;
   int *f_xl = nullptr, *f_iy = nullptr, *f_field = nullptr;
   double* f_val = nullptr;
+  float2* matp = nullptr;  // FP32 packed laminate pairs [nmat][LAMP]
+  // host copies kept for re-planning the task list (autotuner)
+  std::vector<PlateDesc> h_plates;
+  std::vector<int> h_fscen, h_fnode, h_ffield;
+  std::vector<double> h_fval;
+  std::vector<void*> task_allocs;
 };
 
 // ---------------------------------------------------------------------------
@@ -272,6 +284,7 @@ struct shm_plan {
   double sc_k0 = 0, sc_e31 = 0, sc_e32 = 0, sc_hh = 0;
   // structured path
   StructPlan sp;
+  bool sp_generic = false;  // FP32 structured: use the generic template instead of the packed kernel
   // graph
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
@@ -526,6 +539,14 @@ static shm_status set_func_attrs(shm_plan* p) {
                               (int)struct_smem_bytes<float, 32>()));
   CKP(p, cudaFuncSetAttribute(k_struct_step<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_smem_bytes<float, 16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<16>()));
   return SHM_OK;
 }
 
@@ -554,12 +575,91 @@ static double lane_utilisation(const shm_mesh* meshes, int nscen, int EW) {
   return total > 0 ? used / total : 0;
 }
 
+// (re)build the structured task list for EW elements per lane group and H
+// element rows per task; device arrays of a previous list are released
+static shm_status struct_tasks(shm_plan* p, int EW, int H) {
+  StructPlan& sp = p->sp;
+  const int own = 5 * (EW - 1);
+  struct TaskTmp {
+    TaskDesc t;
+    std::vector<int> fxl, fiy, ffield;
+    std::vector<double> fval;
+  };
+  const int nscen = (int)sp.h_plates.size();
+  std::vector<TaskTmp> tasks;
+  std::vector<std::vector<int>> task_index(nscen);
+  for (int s = 0; s < nscen; ++s) {
+    const PlateDesc& pl = sp.h_plates[s];
+    const int ns = (pl.NX + own - 1) / own, nb = (pl.ney + H - 1) / H;
+    task_index[s].assign((size_t)ns * nb, -1);
+    for (int b = 0; b < nb; ++b)
+      for (int k = 0; k < ns; ++k) {
+        TaskTmp t;
+        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};
+        const int last = std::min(H * (b + 1), pl.ney);
+        t.t.nrows = b == 0 ? last : last - (H * b - 1);
+        task_index[s][(size_t)b * ns + k] = (int)tasks.size();
+        tasks.push_back(std::move(t));
+      }
+  }
+  for (size_t q = 0; q < sp.h_fnode.size(); ++q) {
+    const int s = sp.h_fscen[q];
+    const PlateDesc& pl = sp.h_plates[s];
+    const int ns = (pl.NX + own - 1) / own, nb = (pl.ney + H - 1) / H;
+    const int node = sp.h_fnode[q];
+    const int ix = node % pl.NX, iy = node / pl.NX;
+    const int k = ix / own;
+    const int b = std::min(iy / (5 * H), nb - 1);
+    TaskTmp& t = tasks[task_index[s][(size_t)b * ns + k]];
+    t.fxl.push_back(ix - 5 * (k * (EW - 1) - 1));
+    t.fiy.push_back(iy);
+    t.ffield.push_back(sp.h_ffield[q]);
+    t.fval.push_back(sp.h_fval[q]);
+  }
+  // longest tasks first so that lane groups of a CTA stay in step
+  std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
+  std::vector<TaskDesc> td;
+  std::vector<int> fxl, fiy, ffield;
+  std::vector<double> fval;
+  for (TaskTmp& t : tasks) {
+    t.t.f0 = (int)fxl.size();
+    t.t.fn = (int)t.fxl.size();
+    fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
+    fiy.insert(fiy.end(), t.fiy.begin(), t.fiy.end());
+    ffield.insert(ffield.end(), t.ffield.begin(), t.ffield.end());
+    fval.insert(fval.end(), t.fval.begin(), t.fval.end());
+    td.push_back(t.t);
+  }
+  // release the previous list
+  for (void* q : sp.task_allocs) {
+    auto it = std::find(p->allocs.begin(), p->allocs.end(), q);
+    if (it != p->allocs.end()) p->allocs.erase(it);
+    cudaFree(q);
+  }
+  sp.task_allocs.clear();
+  shm_status st;
+  TaskDesc* dt = nullptr;
+  if ((st = upload(p, &dt, td)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_xl, fxl)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_iy, fiy)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_field, ffield)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_val, fval)) != SHM_OK) return st;
+  sp.task_allocs = {dt, sp.f_xl, sp.f_iy, sp.f_field, sp.f_val};
+  sp.tasks = dt;
+  sp.ntask = (int)td.size();
+  sp.tile = EW;
+  sp.H = H;
+  const int G = 32 / EW;
+  sp.grid = (sp.ntask + G - 1) / G;
+  return SHM_OK;
+}
+
 static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, const shm_material* mats,
                                const shm_run* runs, int tile_elems, const std::vector<double>& gw,
                                const std::vector<double>& geo, const std::vector<int>& emat,
                                const std::vector<double>& ekeep, const std::vector<int>& esens,
                                const std::vector<int>& fq_field, const std::vector<double>& fq_val,
-                               std::string& why) {
+                               const std::vector<double>& mat, int rows_per_block, std::string& why) {
   (void)mats;
   (void)fq_field;
   (void)fq_val;
@@ -612,66 +712,24 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
     plates[s] = PlateDesc{nex, ney, NX, s, (long long)p->node_off[s], (long long)egrid, sx, sy, a4};
     egrid += (int64_t)nex * ney;
   }
-  // tile (elements per warp line) and rows per block
+  sp.h_plates = plates;
+  for (int sidx = 0; sidx < nscen; ++sidx)
+    for (int q = 0; q < runs[sidx].n_force; ++q) {
+      const int d = runs[sidx].force_dof[q];
+      sp.h_fscen.push_back(sidx);
+      sp.h_fnode.push_back((d - 1) / 5);
+      sp.h_ffield.push_back((d - 1) % 5);
+      sp.h_fval.push_back(runs[sidx].force_val[q]);
+    }
   int EW = tile_elems;
   if (EW != 16 && EW != 32) EW = lane_utilisation(meshes, nscen, 32) >= 0.9 * lane_utilisation(meshes, nscen, 16) ? 32 : 16;
-  const int own = 5 * (EW - 1);
-  int H = 16;
-  sp.tile = EW;
-  sp.H = H;
-  struct TaskTmp { TaskDesc t; std::vector<int> fxl, fiy, ffield; std::vector<double> fval; };
-  std::vector<TaskTmp> tasks;
-  std::vector<std::vector<int>> task_index(nscen);
-  for (int s = 0; s < nscen; ++s) {
-    const PlateDesc& pl = plates[s];
-    const int ns = (pl.NX + own - 1) / own, nb = (pl.ney + H - 1) / H;
-    task_index[s].assign((size_t)ns * nb, -1);
-    for (int b = 0; b < nb; ++b)
-      for (int k = 0; k < ns; ++k) {
-        TaskTmp t;
-        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};
-        const int last = std::min(H * (b + 1), pl.ney);
-        t.t.nrows = b == 0 ? last : last - (H * b - 1);
-        task_index[s][(size_t)b * ns + k] = (int)tasks.size();
-        tasks.push_back(std::move(t));
-      }
-    for (int q = 0; q < runs[s].n_force; ++q) {
-      const int d = runs[s].force_dof[q];
-      const int node = (d - 1) / 5, field = (d - 1) % 5;
-      const int ix = node % pl.NX, iy = node / pl.NX;
-      const int k = ix / own;
-      const int b = std::min(iy / (5 * H), nb - 1);
-      TaskTmp& t = tasks[task_index[s][(size_t)b * ns + k]];
-      t.fxl.push_back(ix - 5 * (k * (EW - 1) - 1));
-      t.fiy.push_back(iy);
-      t.ffield.push_back(field);
-      t.fval.push_back(runs[s].force_val[q]);
-    }
-  }
-  // longest tasks first so that lane groups of a CTA stay in step
-  std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
-  std::vector<TaskDesc> td;
-  std::vector<int> fxl, fiy, ffield;
-  std::vector<double> fval;
-  for (TaskTmp& t : tasks) {
-    t.t.f0 = (int)fxl.size();
-    t.t.fn = (int)t.fxl.size();
-    fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
-    fiy.insert(fiy.end(), t.fiy.begin(), t.fiy.end());
-    ffield.insert(ffield.end(), t.ffield.begin(), t.ffield.end());
-    fval.insert(fval.end(), t.fval.begin(), t.fval.end());
-    td.push_back(t.t);
-  }
-  sp.ntask = (int)td.size();
   shm_status st;
   {
     PlateDesc* dp = nullptr;
-    TaskDesc* dt = nullptr;
     if ((st = upload(p, &dp, plates)) != SHM_OK) return st;
-    if ((st = upload(p, &dt, td)) != SHM_OK) return st;
     sp.plates = dp;
-    sp.tasks = dt;
   }
+  if ((st = struct_tasks(p, EW, rows_per_block > 0 ? rows_per_block : 16)) != SHM_OK) return st;
   if ((st = upload(p, &sp.emat_g, emat_g)) != SHM_OK) return st;
   if ((st = upload(p, &sp.esens_g, esens_g)) != SHM_OK) return st;
   if (p->prec == 64) {
@@ -684,17 +742,76 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
     if ((st = upload(p, &k, k32)) != SHM_OK) return st;
     sp.ekeep_g = k;
   }
-  if ((st = upload(p, &sp.f_xl, fxl)) != SHM_OK) return st;
-  if ((st = upload(p, &sp.f_iy, fiy)) != SHM_OK) return st;
-  if ((st = upload(p, &sp.f_field, ffield)) != SHM_OK) return st;
-  if ((st = upload(p, &sp.f_val, fval)) != SHM_OK) return st;
-  const int G = 32 / EW;
-  sp.grid = (sp.ntask + G - 1) / G;
+  if (p->prec == 32) {
+    const size_t nmat = mat.size() / MAT_STRIDE_DEV;
+    std::vector<float2> mp(nmat * LAMP);
+    for (size_t m = 0; m < nmat; ++m)
+      for (int c = 0; c < LAMP; ++c)
+        mp[m * LAMP + c] = make_float2((float)mat[m * MAT_STRIDE_DEV + kLamPairs[c][0]],
+                                       (float)mat[m * MAT_STRIDE_DEV + kLamPairs[c][1]]);
+    if ((st = upload(p, &sp.matp, mp)) != SHM_OK) return st;
+  }
   return SHM_OK;
+}
+
+static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s) {
+  StructPlan& sp = p->sp;
+  F32Args a;
+  a.plates = sp.plates;
+  a.tasks = sp.tasks;
+  a.ntask = sp.ntask;
+  a.H = sp.H;
+  a.nn_first = p->nn_first;
+  a.nft = p->nft;
+  a.nnode_pad = p->nnode_pad;
+  a.UA = (float*)p->UA;
+  a.UB = (float*)p->UB;
+  a.minv = (const float*)p->minv;
+  for (int f = 0; f < 5; ++f) {
+    a.k1[f] = (float)p->k1[f];
+    a.k2[f] = (float)p->k2[f];
+  }
+  a.matp = sp.matp;
+  a.emat_g = sp.emat_g;
+  a.ekeep_g = (const float*)sp.ekeep_g;
+  a.esens_g = sp.esens_g;
+  a.f_xl = sp.f_xl;
+  a.f_iy = sp.f_iy;
+  a.f_field = sp.f_field;
+  a.f_val = sp.f_val;
+  a.st = p->st;
+  a.nout = p->nout;
+  a.out_node = p->out_node;
+  a.out_field = p->out_field;
+  a.displ = p->displ;
+  a.vsum = p->vsum;
+  fill_sc(p, a.sc);
+  a.frm_int = p->frm_int;
+  a.frame_field = p->frame_field;
+  a.nframes = p->nframes;
+  a.frames = (float*)p->frames;
+  a.a1 = (float)p->a1;
+  a.blowup = (float)p->blowup;
+  a.flag = p->flag;
+  a.d_base = p->d_base;
+  const bool sens = p->nslot > 0;
+  if (sp.tile == 32) {
+    if (sens)
+      k_struct_step_f32<32, true><<<sp.grid, CTA_THREADS, struct_f32_smem_bytes<32>(), s>>>(a, kstep);
+    else
+      k_struct_step_f32<32, false><<<sp.grid, CTA_THREADS, struct_f32_smem_bytes<32>(), s>>>(a, kstep);
+  } else {
+    if (sens)
+      k_struct_step_f32<16, true><<<sp.grid, CTA_THREADS, struct_f32_smem_bytes<16>(), s>>>(a, kstep);
+    else
+      k_struct_step_f32<16, false><<<sp.grid, CTA_THREADS, struct_f32_smem_bytes<16>(), s>>>(a, kstep);
+  }
+  return cudaGetLastError();
 }
 
 template <typename T>
 static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
+  if (sizeof(T) == 4 && !p->sp_generic) return launch_struct_step_f32(p, kstep, s);
   StructPlan& sp = p->sp;
   StructArgs<T> a;
   a.plates = sp.plates;
@@ -854,6 +971,14 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
     CKP(p, cudaMemcpyToSymbol(c_D32, D32, sizeof(float) * 36));
     CKP(p, cudaMemcpyToSymbol(c_w64, gw.data(), sizeof(double) * 6));
     CKP(p, cudaMemcpyToSymbol(c_w32, w32, sizeof(float) * 6));
+    float2 dp[6][3], dtp[6][3];
+    for (int k = 0; k < 6; ++k)
+      for (int q = 0; q < 3; ++q) {
+        dp[k][q] = make_float2((float)D[(2 * q) * 6 + k], (float)D[(2 * q + 1) * 6 + k]);
+        dtp[k][q] = make_float2((float)D[k * 6 + 2 * q], (float)D[k * 6 + 2 * q + 1]);
+      }
+    CKP(p, cudaMemcpyToSymbol(c_Dp, dp, sizeof(dp)));
+    CKP(p, cudaMemcpyToSymbol(c_DTp, dtp, sizeof(dtp)));
   }
 
   // connectivity, geometry, materials, slots
@@ -1069,13 +1194,14 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
 
   // path selection
   p->path = 1;
-  if (o.path == 2 || o.path == 0) {
+  p->sp_generic = (o.path == 3);
+  if (o.path == 2 || o.path == 0 || o.path == 3) {
     std::string why;
     shm_status ss = struct_build(p, nscen, meshes, mats, runs, o.tile_elems, gw, geo, emat, ekeep, esens, fq_field,
-                                 fq_val, why);
+                                 fq_val, mat, o.rows_per_block, why);
     if (ss == SHM_OK) {
       p->path = 2;
-    } else if (o.path == 2) {
+    } else if (o.path == 2 || o.path == 3) {
       p->err = "structured path not available: " + why;
       return ss == SHM_ERR_OOM || ss == SHM_ERR_CUDA ? ss : SHM_ERR_UNSUPPORTED;
     }
@@ -1368,11 +1494,57 @@ extern "C" shm_status shm_plan_info(const shm_plan* p, int64_t* info) {
   info[5] = p->nframes;
   info[6] = p->path == 2 ? 1 : 2;
   info[7] = p->path == 2 ? p->sp.tile : 0;
+  info[8] = p->path == 2 ? p->sp.H : 0;
   return SHM_OK;
 }
 
 extern "C" shm_status shm_mass(shm_plan* p, double* mg) {
   if (!p || !mg) return SHM_ERR_BAD_ARG;
   std::memcpy(mg, p->mass.data(), sizeof(double) * p->mass.size());
+  return SHM_OK;
+}
+
+static void drop_graph(shm_plan* p) {
+  if (p->gexec) {
+    cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+    p->gsteps = 0;
+  }
+}
+
+extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out, int32_t* rows_out,
+                                   float* ms_out) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (p->path != 2) return bad(p, "autotune: the plan does not use the structured kernel");
+  const int avail = p->nft - p->nn_first + 1;
+  const int warm = 2;
+  steps = std::max(2, std::min(steps, avail - warm));
+  if (steps < 2) return bad(p, "autotune: run too short");
+  const int tiles[2] = {16, 32};
+  const int rows[5] = {4, 8, 16, 32, 64};
+  float best = 1e30f;
+  int bt = p->sp.tile, bh = p->sp.H;
+  for (int ti = 0; ti < 2; ++ti)
+    for (int hi = 0; hi < 5; ++hi) {
+      shm_status st = struct_tasks(p, tiles[ti], rows[hi]);
+      if (st != SHM_OK) return st;
+      drop_graph(p);
+      if ((st = shm_reset(p)) != SHM_OK) return st;
+      if ((st = advance_async(p, warm, p->stream)) != SHM_OK) return st;
+      float ms = 0.f;
+      if ((st = shm_time_steps(p, steps, &ms)) != SHM_OK) return st;
+      if (ms < best) {
+        best = ms;
+        bt = tiles[ti];
+        bh = rows[hi];
+      }
+    }
+  shm_status st = struct_tasks(p, bt, bh);
+  if (st != SHM_OK) return st;
+  drop_graph(p);
+  if ((st = shm_reset(p)) != SHM_OK) return st;
+  if (tile_out) *tile_out = bt;
+  if (rows_out) *rows_out = bh;
+  if (ms_out) *ms_out = best / steps;
   return SHM_OK;
 }

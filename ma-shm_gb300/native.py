@@ -45,7 +45,7 @@ class ShmRun(C.Structure):
 
 class ShmOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("path", C.c_int32), ("steps_per_graph", C.c_int32),
-                ("tile_elems", C.c_int32), ("device", C.c_int32)]
+                ("tile_elems", C.c_int32), ("device", C.c_int32), ("rows_per_block", C.c_int32)]
 
 
 class ShmError(RuntimeError):
@@ -73,6 +73,8 @@ SIGNATURES = {
     "shm_apply_stiffness": (C.c_int, [C.c_void_p, F64P, F64P]),
     "shm_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "shm_mass": (C.c_int, [C.c_void_p, F64P]),
+    "shm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                               C.POINTER(C.c_float)]),
     "shm_stiffness_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }

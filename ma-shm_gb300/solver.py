@@ -53,7 +53,7 @@ class Plan:
     """A set of scenarios advanced together on one GPU (owns the C plan)."""
 
     def __init__(self, scenarios, run: RunConfig, precision: int = 64, path: int = 0,
-                 steps_per_graph: int = 0, tile_elems: int = 0, device: int = 0):
+                 steps_per_graph: int = 0, tile_elems: int = 0, device: int = 0, rows_per_block: int = 0):
         self.lib = native.load()
         self.scenarios = list(scenarios)
         self.run = run
@@ -64,7 +64,7 @@ class Plan:
         runs = (native.ShmRun * n)()
         for i, sc in enumerate(self.scenarios):
             self._fill(sc, meshes[i], mats[i], runs[i])
-        opt = native.ShmOptions(precision, path, steps_per_graph, tile_elems, device)
+        opt = native.ShmOptions(precision, path, steps_per_graph, tile_elems, device, rows_per_block)
         handle = C.c_void_p()
         st = self.lib.shm_plan_create(n, meshes, mats, runs, C.byref(opt), C.byref(handle))
         self.handle = handle
@@ -74,12 +74,22 @@ class Plan:
             self.handle = None
             raise native.ShmError(st, msg)
         self._keep.clear()
-        info = (C.c_int64 * 8)()
-        self.lib.shm_plan_info(self.handle, info)
-        self.info = dict(nnode=info[0], fen=info[1], ndof=info[2], path=info[3], precision=info[4],
-                         nframes=info[5], launches_per_step=info[6], tile=info[7])
+        self._refresh_info()
         self.nscen = n
         self.nft = run.nft
+
+    def _refresh_info(self):
+        info = (C.c_int64 * 9)()
+        self.lib.shm_plan_info(self.handle, info)
+        self.info = dict(nnode=info[0], fen=info[1], ndof=info[2], path=info[3], precision=info[4],
+                         nframes=info[5], launches_per_step=info[6], tile=info[7], rows_per_block=info[8])
+
+    def autotune(self, steps: int = 20):
+        """Pick the structured kernel's lane-group width and rows per task by timing."""
+        t, r, ms = C.c_int32(), C.c_int32(), C.c_float()
+        self._check(self.lib.shm_autotune(self.handle, int(steps), C.byref(t), C.byref(r), C.byref(ms)))
+        self._refresh_info()
+        return dict(tile=t.value, rows_per_block=r.value, ms_per_step=ms.value)
 
     def _arr(self, a, dtype):
         a = np.ascontiguousarray(a, dtype=dtype)

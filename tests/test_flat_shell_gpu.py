@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-10
 FP32_TOL = 1e-3
+FP32_VOLT_TOL = 5e-3
 
 
 def rel(a, b):
@@ -74,7 +75,7 @@ def test_fp32_cfg1_within_tolerance(pkg):
     the derived velocity a1*(u(n+1)-u(n-1)))."""
     scs, run = pkg.workloads.plate_force()
     _, ref = oracle_run(scs[0], run)
-    for path in (1, 2):
+    for path in (1, 2, 3):
         plan = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=64)
         got = plan.forward()[0]
         plan.close()
@@ -130,7 +131,7 @@ def test_apply_stiffness_matches_oracle(pkg):
         assert rel(F, Fo) <= tol, prec
 
 
-@pytest.mark.parametrize("path", [1, 2])
+@pytest.mark.parametrize("path", [1, 2, 3])
 def test_batch_equals_solo(pkg, path):
     """Scenarios of uneven size in one plan give the same bits as solo runs."""
     rng = np.random.default_rng(5)
@@ -157,7 +158,7 @@ def test_batch_equals_solo(pkg, path):
 
 def test_graph_and_resume_are_bit_identical(pkg):
     scs, run = small_case(pkg, nft_cap=300)
-    for path in (1, 2):
+    for path in (1, 2, 3):
         a = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=0)
         ra = a.forward()[0]
         b = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=37)
@@ -177,6 +178,57 @@ def test_graph_and_resume_are_bit_identical(pkg):
         np.testing.assert_array_equal(Uc, Ua)
         for p in (a, b, c):
             p.close()
+
+
+@pytest.mark.parametrize("tile", [16, 32])
+def test_packed_fp32_kernel_matches_oracle(pkg, tile):
+    """Packed FP32x2 structured kernel (path 2) and the generic FP32 template
+    (path 3) on a batch with PZT sensors, damage, frames and two lane-group
+    widths: both within the FP32 bound of the FP64 oracle, and close to each
+    other on the displacement signals."""
+    scs = [pkg.workloads.random_plate(np.random.default_rng([3, s]), edge=6.25e-3, nmin=20, nmax=45)
+           for s in range(3)]
+    dt, nft = 7e-8, 400
+    for sc in scs:
+        _, sc.signal = pkg.hanning_signal(dt, nft, sc.carrier / 5, sc.carrier)
+        sc.sensors = [np.array([5, 6, 7], np.int32)]
+        sc.pzt = dict(pzt_thickness=0.2e-3, g33=1.5e-8, e31=-5.4, e32=-5.4)
+    run = pkg.RunConfig(dt=dt, nft=nft, eta_xy=4e2, eta_z=4e3, h=3.9e-3, frm_int=100)
+    res = {}
+    for path in (2, 3):
+        plan = pkg.Plan(scs, run, precision=32, path=path, tile_elems=tile, steps_per_graph=50)
+        assert plan.info["tile"] == tile
+        res[path] = plan.forward(want_frames=True)
+        plan.close()
+    for s, sc in enumerate(scs):
+        _, ref = oracle_run(sc, run)
+        for path in (2, 3):
+            for key in ("displ", "frames"):
+                assert rel(res[path][s][key], ref[key]) <= FP32_TOL, (path, s, key)
+            # the PZT voltage is a strain measure read as the wave front
+            # arrives; FP32 state error shows up more there than on displacements
+            assert rel(res[path][s]["voltage"], ref["voltage"]) <= FP32_VOLT_TOL, (path, s)
+        assert rel(res[2][s]["displ"], res[3][s]["displ"]) <= 1e-4
+
+
+def test_autotune_picks_a_config_and_keeps_results(pkg):
+    scs = [pkg.workloads.random_plate(np.random.default_rng([4, s]), edge=6.25e-3, nmin=30, nmax=50)
+           for s in range(4)]
+    dt, nft = 7e-8, 120
+    for sc in scs:
+        _, sc.signal = pkg.hanning_signal(dt, nft, sc.carrier / 5, sc.carrier)
+    run = pkg.RunConfig(dt=dt, nft=nft, eta_xy=4e2, eta_z=4e3, h=3.9e-3)
+    plan = pkg.Plan(scs, run, precision=32, path=2, steps_per_graph=20)
+    best = plan.autotune(5)
+    assert best["tile"] in (16, 32) and best["rows_per_block"] in (4, 8, 16, 32, 64)
+    assert plan.info["tile"] == best["tile"] and plan.info["rows_per_block"] == best["rows_per_block"]
+    tuned = plan.forward()
+    plan.close()
+    ref = pkg.Plan(scs, run, precision=32, path=2, tile_elems=best["tile"], rows_per_block=best["rows_per_block"])
+    again = ref.forward()
+    ref.close()
+    for a, b in zip(tuned, again):
+        np.testing.assert_array_equal(a["displ"], b["displ"])
 
 
 def test_divergence_is_reported(pkg):
