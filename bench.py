@@ -146,6 +146,74 @@ def cpu_reference(scenarios, run, steps, nthreads=0, budget_s=20.0):
     return done_dof_steps / t_total, used, t_total
 
 
+def adjoint_bench(pkg, args):
+    """Gradient cost / forward cost on the damage-identification batch, FP32
+    gradient vs FP64 gradient, and central differences on 20 parameters."""
+    import torch
+    W = pkg.workloads
+    scs, run, hidden = W.adjoint_maps(n=args.adj_maps, nft=args.adj_steps)
+    # targets from the hidden maps (FP64 forward)
+    truth = [pkg.Scenario(**{**sc.__dict__, "elem_keep": h}) for sc, h in zip(scs, hidden)]
+    p64 = pkg.Plan(truth, run, precision=64, path=1, steps_per_graph=50)
+    targets = [r["displ"] for r in p64.forward()]
+    p64.close()
+    ndof = W.dof_count(scs)
+    out = {"metric": "adjoint gradient cost / forward cost", "maps": len(scs), "dof": ndof, "nft": run.nft,
+           "ckpt_every": 200, "dtype": "f32 stepping, f64 misfit and gradient"}
+    times = {}
+    for path in (1, 2):
+        p = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=50)
+        p.forward()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p.forward()
+        torch.cuda.synchronize()
+        times[path] = time.perf_counter() - t0
+        if path == 1:
+            t0 = time.perf_counter()
+            mis32, g32 = p.forward_backward(targets, ckpt_every=200)
+            torch.cuda.synchronize()
+            t_adj = time.perf_counter() - t0
+        p.close()
+    out["forward_s_general_path"] = times[1]
+    out["forward_s_structured_path"] = times[2]
+    out["forward_backward_s"] = t_adj
+    out["ratio_vs_forward_same_path"] = t_adj / times[1]
+    out["ratio_vs_fastest_forward"] = t_adj / min(times.values())
+    # FP64 reference gradient on the first maps
+    nref = min(4, len(scs))
+    p = pkg.Plan(scs[:nref], run, precision=64, path=1)
+    mis64, g64 = p.forward_backward(targets[:nref], ckpt_every=200)
+    p.close()
+    out["grad_rel_err_f32_vs_f64"] = max(float(np.linalg.norm(g32[i] - g64[i]) / np.linalg.norm(g64[i]))
+                                         for i in range(nref))
+    out["misfit_rel_err_f32_vs_f64"] = max(float(abs(mis32[i] - mis64[i]) / mis64[i]) for i in range(nref))
+    # central differences (FP64 forward) on 20 random parameters of map 0
+    rng = np.random.default_rng(7)
+    idx = rng.choice(len(g64[0]), 20, replace=False)
+    eps = 1e-4
+    sc0 = scs[0]
+
+    def J(keep):
+        q = pkg.Plan([pkg.Scenario(**{**sc0.__dict__, "elem_keep": keep})], run, precision=64, path=1,
+                     steps_per_graph=50)
+        d = q.forward()[0]["displ"]
+        q.close()
+        r = (d - targets[0])[run.nn_first - 1:]
+        return 0.5 * float(np.sum(r * r))
+
+    fd = []
+    for e in idx:
+        kp, km = sc0.elem_keep.copy(), sc0.elem_keep.copy()
+        kp[e] -= eps
+        km[e] += eps
+        fd.append((J(kp) - J(km)) / (2 * eps))
+    fd = np.array(fd)
+    out["fd_rel_err_f64_grad"] = float(np.linalg.norm(g64[0][idx] - fd) / np.linalg.norm(fd))
+    out["fd_rel_err_f32_grad"] = float(np.linalg.norm(g32[0][idx] - fd) / np.linalg.norm(fd))
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -160,12 +228,17 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--adjoint", action="store_true", help="damage-gradient workload instead of the forward batch")
+    ap.add_argument("--adj-maps", type=int, default=64)
+    ap.add_argument("--adj-steps", type=int, default=20000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     rank, ws, local = dist_init(args)
     import __graft_entry__ as g
     pkg = g.package()
+    if args.adjoint:
+        return adjoint_bench(pkg, args)
     W = pkg.workloads
     scs, run = W.batch(n=args.plates, seed=1000 * rank)
     ndof = W.dof_count(scs)

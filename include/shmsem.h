@@ -138,6 +138,19 @@ shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
  * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task. */
 shm_status shm_plan_info(const shm_plan *plan, int64_t *info9);
 
+/* Discrete adjoint of the whole forward solve (no counterpart in the
+ * reference, which has no gradients).  Misfit per scenario
+ *   J = 1/2 sum_q sum_{nn=nn_first..nft} (displ(nn,q) - target(nn,q))^2
+ * with displ as in shm_forward; grad[e] = dJ/dd_e for every element of every
+ * scenario (concatenated), where the element stiffness is (1 - d_e) K_e^0, i.e.
+ * d_e = 1 - elem_keep.  The forward pass keeps (u_n, u_{n-1}) every
+ * `ckpt_every` steps, each segment is recomputed forward and the adjoint
+ * lambda is stepped back through it with the same element operator; misfit
+ * and gradient are accumulated in FP64.  Uses the general kernels.
+ *   target [nscen][nft x n_out] column-major per scenario, like displ. */
+shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *target, double *misfit,
+                                double *grad, int32_t ckpt_every, void *stream);
+
 /* Autotuner of the structured kernel: times `steps` steps for every
  * (elements per lane group, element rows per task) candidate -- {16, 32} x
  * {4, 8, 16, 32, 64} -- re-planning the task list each time, keeps the

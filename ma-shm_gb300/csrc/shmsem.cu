@@ -70,6 +70,12 @@ template <typename T> struct GenArgs {
   T blowup;                       // 10*h
   int* flag;
   const int* d_base;
+  // adjoint (k_elem_adjoint only)
+  int nadj;                       // adjoint force slots, one per point output
+  const double* __restrict__ asig;  // [nout][nft] misfit residuals in reversed time
+  const T* __restrict__ seg;      // forward states of the current segment [k][5][nnode_pad]
+  int seg_base;                   // segment slice = seg_base - nn
+  double* grad;                   // [fen_pad] dJ/dd_e accumulated in FP64
 };
 
 template <typename T>
@@ -150,6 +156,90 @@ __global__ void __launch_bounds__(CTA_THREADS) k_elem_general(GenArgs<T> a, int 
       for (int i = 0; i < NP; ++i) s += (double)vred[i * CTA_ELEMS + le];
       a.vsum[(int64_t)slot * a.nft + (nn - 1)] = s;
     }
+  }
+}
+
+// Adjoint step, element part (general path).  Applies K_e^0 to lambda_{n}
+// (current), writes keep_e * K_e^0 lambda to the scratch like the forward
+// step, adds the misfit residuals r(n-1) at the point outputs as forces and
+// accumulates the damage gradient dJ/dd_e -= lambda_n' K_e^0 u_{n-1} with the
+// forward state u_{n-1} of the current checkpoint segment.
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS) k_elem_adjoint(GenArgs<T> a, int kstep) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int nn = *a.d_base + kstep;
+  const T* __restrict__ cur = ((nn - a.nn_first) & 1) ? a.UB : a.UA;
+  if (blockIdx.x == 0) {
+    const int64_t p36 = (int64_t)NPE * a.fen_pad;
+    for (int q = threadIdx.x; q < a.nforce; q += blockDim.x)
+#pragma unroll
+      for (int f = 0; f < 5; ++f) a.F2[f * a.plane + p36 + q] = T(0);
+    for (int q = threadIdx.x; q < a.nadj; q += blockDim.x) {
+      const T v = (T)a.asig[(int64_t)q * a.nft + (nn - 1)];
+#pragma unroll
+      for (int f = 0; f < 5; ++f) a.F2[f * a.plane + p36 + a.nforce + q] = (f == a.out_field[q]) ? v : T(0);
+    }
+  }
+  const int j = threadIdx.x >> 5;
+  const int le = threadIdx.x & 31;
+  const int e = blockIdx.x * CTA_ELEMS + le;
+  T* xs = sm + le * ELEM_STRIDE;
+  T* ys = sm + (CTA_ELEMS + le) * ELEM_STRIDE;
+  T* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
+  {
+    T u[5][NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int node = a.conn[(int64_t)(j * NP + i) * a.fen_pad + e];
+#pragma unroll
+      for (int f = 0; f < 5; ++f) u[f][i] = cur[f * a.nnode_pad + node];
+    }
+    row_deriv_store(u, xs, ys, j);
+  }
+  __syncthreads();
+  {
+    const int i = j;
+    T v[5][NP];
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+#pragma unroll
+      for (int k = 0; k < NP; ++k) v[f][k] = xs[f * NPE + i * NP + k];
+    const Lam<T> L = load_lam(a.mat + (int64_t)a.emat[e] * MAT_STRIDE_DEV, T(1));  // K_e^0
+    GeoGeneral<T> geo{a.geo, a.fen_pad, e};
+    T Fe[5][NP];
+    shell_column<T, GeoGeneral<T>, false>(v, ys, xs, i, L, geo, Fe, a.sc);
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+#pragma unroll
+      for (int m = 0; m < NP; ++m) ys[f * NPE + i * NP + m] = Fe[f][m];
+  }
+  __syncthreads();
+  T out[5][NP];
+  row_transpose_apply(xs, ys, j, out);
+  // gradient partial: (K_e^0 lambda)' u_{n-1} over the row's nodes
+  const T* __restrict__ um = a.seg + (int64_t)(a.seg_base - nn) * 5 * a.nnode_pad;
+  double dot = 0.0;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const int node = a.conn[(int64_t)(j * NP + i) * a.fen_pad + e];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) dot += (double)out[f][i] * (double)um[f * a.nnode_pad + node];
+  }
+  const T keep = a.ekeep[e];
+#pragma unroll
+  for (int f = 0; f < 5; ++f)
+#pragma unroll
+    for (int i = 0; i < NP; ++i) a.F2[f * a.plane + (int64_t)(j * NP + i) * a.fen_pad + e] = keep * out[f][i];
+  double* dred = reinterpret_cast<double*>(vred);
+  __syncthreads();  // vred region is free (phase B of this kernel does not use it)
+  dred[j * CTA_ELEMS + le] = dot;
+  __syncthreads();
+  if (j == 0 && e < a.fen) {
+    double sgr = 0.0;
+#pragma unroll
+    for (int r = 0; r < NP; ++r) sgr += dred[r * CTA_ELEMS + le];
+    a.grad[e] -= sgr;
   }
 }
 
@@ -285,6 +375,11 @@ struct shm_plan {
   // structured path
   StructPlan sp;
   bool sp_generic = false;  // FP32 structured: use the generic template instead of the packed kernel
+  // adjoint buffers (allocated by the first shm_forward_backward)
+  void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr;
+  double *grad = nullptr, *asig = nullptr;
+  int* d_base_adj = nullptr;
+  int seg_k = 0, nck = 0;
   // graph
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
@@ -503,6 +598,11 @@ static size_t elem_smem_bytes(int prec) {
   return ts * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS);
 }
 
+static size_t adj_smem_bytes(int prec) {
+  const size_t ts = prec == 64 ? 8 : 4;
+  return ts * (2 * CTA_ELEMS * ELEM_STRIDE) + sizeof(double) * NP * CTA_ELEMS;
+}
+
 template <typename T>
 static cudaError_t launch_general_step(shm_plan* p, int kstep, cudaStream_t s) {
   GenArgs<T> a = make_args<T>(p);
@@ -531,6 +631,10 @@ static shm_status set_func_attrs(shm_plan* p) {
   CKP(p, cudaFuncSetAttribute(k_elem_general<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
   CKP(p, cudaFuncSetAttribute(k_elem_general<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
   CKP(p, cudaFuncSetAttribute(k_elem_general<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+  CKP(p, cudaFuncSetAttribute(k_elem_adjoint<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)adj_smem_bytes(64)));
+  CKP(p, cudaFuncSetAttribute(k_elem_adjoint<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)adj_smem_bytes(32)));
   CKP(p, cudaFuncSetAttribute(k_struct_step<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_smem_bytes<double, 32>()));
   CKP(p, cudaFuncSetAttribute(k_struct_step<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1011,7 +1115,7 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
         node_cnt[p->node_off[s] + nd - 1]++;
       }
   }
-  int nforce_tot = 0;
+  int nforce_tot = 0, nout_tot = 0;
   for (int s = 0; s < nscen; ++s) {
     if (runs[s].n_force < 0 || (runs[s].n_force > 0 && (!runs[s].force_dof || !runs[s].force_val)))
       return bad(p, "run: bad excitation arrays");
@@ -1021,18 +1125,25 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
       node_cnt[p->node_off[s] + (d - 1) / 5]++;
     }
     nforce_tot += runs[s].n_force;
+    if (runs[s].n_out < 0 || (runs[s].n_out > 0 && !runs[s].out_dof)) return bad(p, "run: bad output arrays");
+    for (int q = 0; q < runs[s].n_out; ++q) {
+      const int d = runs[s].out_dof[q];
+      if (d < 1 || d > 5 * meshes[s].nnode) return bad(p, "run: output DOF out of range");
+      node_cnt[p->node_off[s] + (d - 1) / 5]++;  // adjoint force slot of this output
+      nout_tot++;
+    }
   }
   p->nforce = nforce_tot;
   for (int64_t g = 0; g < p->nnode; ++g) row_ptr[g + 1] = row_ptr[g] + node_cnt[g];
   slots.assign(row_ptr[p->nnode], 0);
   std::vector<int> fillc(p->nnode, 0);
   const int64_t P36 = (int64_t)NPE * FP;
-  p->plane = P36 + std::max(nforce_tot, 1);
+  p->plane = P36 + std::max(nforce_tot + nout_tot, 1);
   p->plane = (p->plane + 31) / 32 * 32;
 
   std::vector<int> fq_field, fq_scen;
   std::vector<double> fq_val;
-  int fq = 0;
+  int fq = 0, fo = 0;
   for (int s = 0; s < nscen; ++s) {
     const shm_mesh& m = meshes[s];
     const shm_material& mt = mats[s];
@@ -1110,6 +1221,13 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
       fq_scen.push_back(s);
       fq_val.push_back(runs[s].force_val[q]);
       ++fq;
+    }
+    // adjoint force slots (misfit residuals at the point outputs) after them
+    for (int q = 0; q < runs[s].n_out; ++q) {
+      const int d = runs[s].out_dof[q];
+      const int64_t g = n0 + (d - 1) / 5;
+      if (fillc[g] >= node_cnt[g]) return bad(p, "internal: slot overflow");
+      slots[row_ptr[g] + fillc[g]++] = (int)(P36 + nforce_tot + fo++);
     }
   }
   for (int64_t g = 0; g < p->nnode; ++g)
@@ -1547,4 +1665,140 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
   if (rows_out) *rows_out = bh;
   if (ms_out) *ms_out = best / steps;
   return SHM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// discrete adjoint: misfit gradient with respect to per-element damage
+// ---------------------------------------------------------------------------
+
+template <typename T>
+static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target, double* misfit, double* grad,
+                            int k, cudaStream_t s) {
+  const int n0 = p->nn_first, N = p->nft;
+  const int nsteps = N - n0 + 1;
+  k = std::max(1, std::min(k, nsteps));
+  const int nck = (nsteps + k - 1) / k;
+  const size_t S = (size_t)5 * p->nnode_pad;
+  shm_status st_;
+  if (!p->LA) {
+    T *la = nullptr, *lb = nullptr;
+    if ((st_ = dalloc(p, &la, S)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &lb, S)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &p->grad, (size_t)p->fen_pad)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &p->asig, (size_t)std::max(p->nout, 1) * p->nft)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &p->d_base_adj, 4)) != SHM_OK) return st_;
+    p->LA = la;
+    p->LB = lb;
+  }
+  if (p->seg_k < k) {
+    T* sg = nullptr;
+    if ((st_ = dalloc(p, &sg, (size_t)k * S)) != SHM_OK) return st_;
+    p->seg = sg;
+    p->seg_k = k;
+  }
+  if (p->nck < nck) {
+    T* c = nullptr;
+    if ((st_ = dalloc(p, &c, (size_t)nck * 2 * S)) != SHM_OK) return st_;
+    p->ck = c;
+    p->nck = nck;
+  }
+  T* UA = (T*)p->UA;
+  T* UB = (T*)p->UB;
+  T* ck = (T*)p->ck;
+  T* seg = (T*)p->seg;
+  const size_t SB = S * sizeof(T);
+  // 1. forward pass, checkpoint (u_n, u_{n-1}) every k steps
+  if ((st_ = shm_reset(p)) != SHM_OK) return st_;
+  if ((st_ = shm_set_signal(p, st, s)) != SHM_OK) return st_;
+  for (int j = 0; j < nck; ++j) {
+    const int n = n0 + j * k;
+    const bool odd = ((n - n0) & 1);
+    CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S, odd ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
+    CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S + S, odd ? UA : UB, SB, cudaMemcpyDeviceToDevice, s));
+    const int cnt = std::min(k, N - n + 1);
+    for (int kk = 0; kk < cnt; ++kk) CKP(p, launch_general_step<T>(p, kk, s));
+    k_advance<<<1, 1, 0, s>>>(p->d_base, cnt);
+  }
+  // 2. misfit (FP64) and the residuals in reversed time
+  std::vector<double> disp((size_t)std::max(p->nout, 1) * N);
+  CKP(p, cudaMemcpyAsync(disp.data(), p->displ, sizeof(double) * disp.size(), cudaMemcpyDeviceToHost, s));
+  CKP(p, cudaStreamSynchronize(s));
+  std::vector<double> asig((size_t)std::max(p->nout, 1) * N, 0.0);
+  for (int sc = 0; sc < p->nscen; ++sc) {
+    double J = 0.0;
+    for (int q = p->out_off[sc]; q < p->out_off[sc + 1]; ++q)
+      for (int m = n0; m <= N; ++m) {
+        const double r = disp[(size_t)q * N + m - 1] - target[(size_t)q * N + m - 1];
+        J += 0.5 * r * r;
+        asig[(size_t)q * N + (N + n0 - m) - 1] = r;  // sample read by the adjoint step t' = N + n0 - m
+      }
+    if (misfit) misfit[sc] = J;
+  }
+  CKP(p, cudaMemcpyAsync(p->asig, asig.data(), sizeof(double) * asig.size(), cudaMemcpyHostToDevice, s));
+  // 3. backward: recompute each segment forward, then step the adjoint back through it
+  CKP(p, cudaMemsetAsync(p->LA, 0, SB, s));
+  CKP(p, cudaMemsetAsync(p->LB, 0, SB, s));
+  CKP(p, cudaMemsetAsync(p->grad, 0, sizeof(double) * p->fen_pad, s));
+  CKP(p, cudaMemcpyAsync(p->d_base_adj, &n0, 4, cudaMemcpyHostToDevice, s));
+  GenArgs<T> a = make_args<T>(p);
+  a.UA = (T*)p->LA;
+  a.UB = (T*)p->LB;
+  a.d_base = p->d_base_adj;
+  a.nadj = p->nout;
+  a.asig = p->asig;
+  a.seg = seg;
+  a.grad = p->grad;
+  a.frm_int = 0;
+  a.nout = 0;
+  const int nblk = (int)(p->fen_pad / CTA_ELEMS);
+  const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
+  std::vector<int> hbase(1);
+  for (int j = nck - 1; j >= 0; --j) {
+    const int sj = n0 + j * k, ej = std::min(sj + k - 1, N);
+    const bool odd = ((sj - n0) & 1);
+    CKP(p, cudaMemcpyAsync(odd ? UB : UA, ck + (size_t)j * 2 * S, SB, cudaMemcpyDeviceToDevice, s));
+    CKP(p, cudaMemcpyAsync(odd ? UA : UB, ck + (size_t)j * 2 * S + S, SB, cudaMemcpyDeviceToDevice, s));
+    hbase[0] = sj;
+    CKP(p, cudaMemcpyAsync(p->d_base, hbase.data(), 4, cudaMemcpyHostToDevice, s));
+    // the forward recompute must not see the adjoint residual forces
+    for (int f = 0; f < 5; ++f)
+      CKP(p, cudaMemsetAsync((T*)p->F2 + f * p->plane + (int64_t)NPE * p->fen_pad + p->nforce, 0,
+                             sizeof(T) * p->nout, s));
+    for (int n = sj; n <= ej; ++n) {
+      const bool o2 = ((n - n0) & 1);
+      CKP(p, cudaMemcpyAsync(seg + (size_t)(n - sj) * S, o2 ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
+      if (n < ej) CKP(p, launch_general_step<T>(p, n - sj, s));
+    }
+    a.seg_base = N + n0 - sj;
+    const int cnt = ej - sj + 1;
+    for (int kk = 0; kk < cnt; ++kk) {
+      k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, s>>>(a, kk);
+      k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kk);
+    }
+    k_advance<<<1, 1, 0, s>>>(p->d_base_adj, cnt);
+    CKP(p, cudaGetLastError());
+    CKP(p, cudaStreamSynchronize(s));  // hbase is reused by the next segment
+  }
+  std::vector<double> g((size_t)p->fen_pad);
+  CKP(p, cudaMemcpyAsync(g.data(), p->grad, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
+  // leave the adjoint slots zero for later forward runs
+  const int64_t p36 = (int64_t)NPE * p->fen_pad;
+  for (int f = 0; f < 5; ++f)
+    if (p->nout > 0)
+      CKP(p, cudaMemsetAsync((T*)p->F2 + f * p->plane + p36 + p->nforce, 0, sizeof(T) * p->nout, s));
+  CKP(p, cudaStreamSynchronize(s));
+  if (grad) std::memcpy(grad, g.data(), sizeof(double) * p->fen);
+  shm_status div = check_flag(p, s);
+  st_ = shm_reset(p);
+  return div != SHM_OK ? div : st_;
+}
+
+extern "C" shm_status shm_forward_backward(shm_plan* p, const double* st, const double* target, double* misfit,
+                                           double* grad, int32_t ckpt_every, void* stream) {
+  if (!p || !st || !target) return SHM_ERR_BAD_ARG;
+  if (p->nout < 1) return bad(p, "forward_backward: the misfit needs point outputs");
+  cudaStream_t s = pick_stream(p, stream);
+  drop_graph(p);
+  return p->prec == 64 ? fwd_bwd_t<double>(p, st, target, misfit, grad, ckpt_every, s)
+                       : fwd_bwd_t<float>(p, st, target, misfit, grad, ckpt_every, s);
 }

@@ -73,6 +73,7 @@ SIGNATURES = {
     "shm_apply_stiffness": (C.c_int, [C.c_void_p, F64P, F64P]),
     "shm_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "shm_mass": (C.c_int, [C.c_void_p, F64P]),
+    "shm_forward_backward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_int32, C.c_void_p]),
     "shm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_float)]),
     "shm_stiffness_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

@@ -91,6 +91,23 @@ class Plan:
         self._refresh_info()
         return dict(tile=t.value, rows_per_block=r.value, ms_per_step=ms.value)
 
+    def forward_backward(self, target, signals=None, ckpt_every: int = 200):
+        """Misfit J (per scenario) and dJ/dd_e (d_e = 1 - elem_keep) by the
+        discrete adjoint with checkpoints every ``ckpt_every`` steps.
+        ``target`` is a list of [nft, n_out] arrays (one per scenario)."""
+        st = np.ascontiguousarray(self.signals() if signals is None else signals, dtype=np.float64)
+        tgt = np.concatenate([np.asarray(t, float).T.reshape(-1) for t in target]) if len(target) else np.zeros(1)
+        mis = np.zeros(self.nscen)
+        grad = np.zeros(self.info["fen"])
+        self._check(self.lib.shm_forward_backward(self.handle, native.ptr(st), native.ptr(tgt), native.ptr(mis),
+                                                  native.ptr(grad), int(ckpt_every), None))
+        out, e0 = [], 0
+        for sc in self.scenarios:
+            fen = np.asarray(sc.mesh["nodes"]).shape[0]
+            out.append(grad[e0:e0 + fen].copy())
+            e0 += fen
+        return mis, out
+
     def _arr(self, a, dtype):
         a = np.ascontiguousarray(a, dtype=dtype)
         self._keep.append(a)

@@ -97,3 +97,30 @@ def batch(n=512, seed=0, T=0.4e-3, edge=6.25e-3, nmin=40, nmax=80, nft=None):
 
 def dof_count(scenarios) -> int:
     return int(sum(5 * np.asarray(s.mesh["coords"]).shape[0] for s in scenarios))
+
+
+def adjoint_maps(n=64, nex=50, L=0.5, nft=20000, f=50e3, seed=0, n_out=8):
+    """Damage-identification batch: n plates with hidden maps of two
+    elliptical zones at 50 % stiffness reduction; the model starts undamaged.
+    Returns (model scenarios, run, hidden keep vectors)."""
+    lam = M.cfrp_laminate()
+    mesh = MS.structured_plate(L, L, nex, nex)
+    dt = _dt_for(L / nex, L / nex, [lam])
+    _, st = hanning_signal(dt, nft, f / 5, f, 0.0)
+    fen = nex * nex
+    centre = MS.nearest_node(mesh["coords"], L / 2, L / 2)
+    outs = MS.circle_sensor_nodes(mesh, L / 2, L / 2, 0.3 * L, n_out)
+    scs, hidden = [], []
+    for s in range(n):
+        rng = np.random.default_rng([seed, s])
+        keep = np.ones(fen)
+        for _ in range(2):
+            xc, yc = rng.uniform(0.2, 0.8, 2) * L
+            a, b = rng.uniform(0.03, 0.08, 2) * L
+            keep[MS.elements_in_ellipse(mesh, xc, yc, a, b, rng.uniform(0, np.pi))] = 0.5
+        hidden.append(keep)
+        scs.append(Scenario(mesh=mesh, mat_table=M.table_row(lam)[None, :], elem_keep=np.ones(fen),
+                            force_dof=np.array([5 * centre], np.int32), force_val=np.array([1.0]),
+                            out_dof=(5 * outs).astype(np.int32), signal=st))
+    run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return scs, run, hidden
