@@ -214,6 +214,44 @@ def adjoint_bench(pkg, args):
     print(json.dumps(out))
 
 
+def single_plate_bench(pkg, args):
+    """One plate (config 1 or 2): whole forward solve in FP64 and FP32 through
+    shm_forward (outputs, PZT voltage, frames), FP32 error vs the FP64 run."""
+    import torch
+    W = pkg.workloads
+    scs, run = W.plate_force() if args.workload == "force" else W.plate_pzt()
+    ndof = W.dof_count(scs)
+    nsteps = run.nft - run.nn_first + 1
+    res, out = {}, {"workload": args.workload, "dof": ndof, "nft": run.nft, "dt_s": run.dt,
+                    "frames": run.frm_int > 0}
+    for prec in (64, 32):
+        p = pkg.Plan(scs, run, precision=prec, path=0, steps_per_graph=50)
+        if p.info["path"] == 2 and prec == 32:
+            out["autotune"] = p.autotune(10)
+        p.forward(want_frames=run.frm_int > 0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = p.forward(want_frames=run.frm_int > 0)[0]
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        res[prec] = r
+        out[f"fp{prec}_dof_steps_per_s"] = ndof * nsteps / dt
+        out[f"fp{prec}_s"] = dt
+        out[f"fp{prec}_path"] = p.info["path"]
+        p.close()
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    out["fp32_vs_fp64_displ_rel_l2"] = rel(res[32]["displ"], res[64]["displ"])
+    vel32 = np.diff(res[32]["displ"][1:], axis=0)
+    vel64 = np.diff(res[64]["displ"][1:], axis=0)
+    out["fp32_vs_fp64_velocity_rel_l2"] = rel(vel32, vel64)
+    if res[64]["voltage"].size and np.abs(res[64]["voltage"]).max() > 0:
+        out["fp32_vs_fp64_voltage_rel_l2"] = rel(res[32]["voltage"], res[64]["voltage"])
+    if "frames" in res[64]:
+        out["fp32_vs_fp64_frames_rel_l2"] = rel(res[32]["frames"], res[64]["frames"])
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -226,9 +264,12 @@ def main():
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general, 2 structured, 3 structured generic")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adjoint", action="store_true", help="damage-gradient workload instead of the forward batch")
+    ap.add_argument("--workload", choices=("batch", "force", "pzt"), default="batch",
+                    help="batch: 512 plates (default); force: 20x20-element plate; pzt: 200x200 plate with PZT")
     ap.add_argument("--adj-maps", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=20000)
     args = ap.parse_args()
@@ -239,6 +280,8 @@ def main():
     pkg = g.package()
     if args.adjoint:
         return adjoint_bench(pkg, args)
+    if args.workload != "batch":
+        return single_plate_bench(pkg, args)
     W = pkg.workloads
     scs, run = W.batch(n=args.plates, seed=1000 * rank)
     ndof = W.dof_count(scs)
@@ -267,11 +310,12 @@ def main():
         return
 
     import torch
-    plan = pkg.Plan(scs, run, precision=args.precision, path=0, steps_per_graph=args.graph,
+    plan = pkg.Plan(scs, run, precision=args.precision, path=args.path, steps_per_graph=args.graph,
                     tile_elems=args.tile, device=local, rows_per_block=args.rows)
     tuned = None
     if plan.info["path"] == 2 and args.tile == 0 and args.rows == 0 and not args.no_tune:
         tuned = plan.autotune(10)
+    config["path"] = "general" if plan.info["path"] == 1 else "structured"
     config["tile_elems"] = plan.info["tile"]
     config["rows_per_block"] = plan.info["rows_per_block"]
     config["autotuned"] = tuned is not None

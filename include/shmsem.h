@@ -151,10 +151,12 @@ shm_status shm_plan_info(const shm_plan *plan, int64_t *info9);
 shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *target, double *misfit,
                                 double *grad, int32_t ckpt_every, void *stream);
 
-/* Autotuner of the structured kernel: times `steps` steps for every
- * (elements per lane group, element rows per task) candidate -- {16, 32} x
- * {4, 8, 16, 32, 64} -- re-planning the task list each time, keeps the
- * fastest and resets the state.  Returns the choice and its ms per step. */
+/* Autotuner for plans on the structured path: times `steps` steps of the
+ * general kernels and of every (elements per lane group, element rows per
+ * task) candidate of the structured kernel -- {16, 32} x {4, 8, 16, 32, 64} --
+ * re-planning the task list each time, keeps the fastest and resets the
+ * state.  Returns the choice (tile_elems = 0: general kernels) and its ms per
+ * step. */
 shm_status shm_autotune(shm_plan *plan, int32_t steps, int32_t *tile_elems, int32_t *rows_per_block,
                         float *ms_per_step);
 

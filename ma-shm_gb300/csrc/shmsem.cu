@@ -1642,6 +1642,19 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
   const int rows[5] = {4, 8, 16, 32, 64};
   float best = 1e30f;
   int bt = p->sp.tile, bh = p->sp.H;
+  // candidate 0: the general element + node kernels
+  {
+    p->path = 1;
+    drop_graph(p);
+    shm_status st = shm_reset(p);
+    if (st == SHM_OK) st = advance_async(p, warm, p->stream);
+    float ms = 0.f;
+    if (st == SHM_OK) st = shm_time_steps(p, steps, &ms);
+    if (st != SHM_OK) return st;
+    best = ms;
+    bt = 0;
+    p->path = 2;
+  }
   for (int ti = 0; ti < 2; ++ti)
     for (int hi = 0; hi < 5; ++hi) {
       shm_status st = struct_tasks(p, tiles[ti], rows[hi]);
@@ -1657,8 +1670,12 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
         bh = rows[hi];
       }
     }
-  shm_status st = struct_tasks(p, bt, bh);
-  if (st != SHM_OK) return st;
+  shm_status st = SHM_OK;
+  if (bt == 0) {
+    p->path = 1;  // the general kernels were fastest
+  } else if ((st = struct_tasks(p, bt, bh)) != SHM_OK) {
+    return st;
+  }
   drop_graph(p);
   if ((st = shm_reset(p)) != SHM_OK) return st;
   if (tile_out) *tile_out = bt;

@@ -124,3 +124,33 @@ def adjoint_maps(n=64, nex=50, L=0.5, nft=20000, f=50e3, seed=0, n_out=8):
                             out_dof=(5 * outs).astype(np.int32), signal=st))
     run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
     return scs, run, hidden
+
+
+def plate_pzt(nex=200, L=1.0, T=1e-3, f=100e3, d_pzt=10e-3, t_pzt=0.2e-3, V0=100.0, n_out=16, radius=0.15,
+              frames_every=100, nft=None):
+    """Config 2: plate with a centred PZT disc acting as actuator (equivalent
+    electromechanical loads, pzt.actuator_loads) and as sensor (voltage),
+    w-velocity frames every ``frames_every`` steps, ``n_out`` point outputs."""
+    from . import pzt as PZ
+    lam = M.cfrp_laminate()
+    mesh = MS.structured_plate(L, L, nex, nex)
+    p = M.pzt5a()
+    pm = M.pzt_material(p["S"], p["d"], p["epsT"], 0.0)
+    elems = MS.elements_in_disc(mesh, L / 2, L / 2, d_pzt / 2)
+    lam_p = M.add_piezo_layer(lam, pm["Qpzt"], p["rho"], t_pzt)
+    table = np.stack([M.table_row(lam), M.table_row(lam_p)])
+    elem_mat = np.zeros(nex * nex, np.int32)
+    elem_mat[elems] = 1
+    Fa = PZ.actuator_loads(mesh, elems, t_pzt, lam["h"], V0, pm["epzt"], pm["gpzt"])
+    nzi = np.nonzero(Fa)[0]
+    dt = _dt_for(L / nex, L / nex, [lam, lam_p])
+    if nft is None:
+        nft = int(np.ceil(T / dt)) + 1
+    _, st = hanning_signal(dt, nft, f / 5, f, 0.0)
+    outs = MS.circle_sensor_nodes(mesh, L / 2, L / 2, min(radius, 0.45 * L), n_out)
+    sc = Scenario(mesh=mesh, mat_table=table, elem_mat=elem_mat, force_dof=(nzi + 1).astype(np.int32),
+                  force_val=Fa[nzi], out_dof=(5 * outs).astype(np.int32), signal=st, sensors=[elems],
+                  pzt=dict(pzt_thickness=t_pzt, g33=pm["g33"], e31=pm["e31"], e32=pm["e32"]))
+    run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"], frm_int=frames_every,
+                    frame_dof=5)
+    return [sc], run

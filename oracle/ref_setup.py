@@ -389,3 +389,182 @@ def mass_vector(WWDetJ, m11, I11, G, L, ndof):
     mgL[3::5] = WWDetJ * I11
     mgL[4::5] = WWDetJ * m11
     return basket_scatter(mgL, G, L, ndof)
+
+
+# --------------------------------------------------------------------------
+# PZT actuator equivalent loads (main_flat_shell.m:144-225)
+# --------------------------------------------------------------------------
+
+
+def shape3d_prim(nx, ny, nz, Qx, Qy, Qz, x, y, z):
+    """``src/models/common/shape3D_prim_v2.m``: derivatives of the nx*ny*nz
+    shape functions (x fastest) at one point, |v| < 1e-12 -> 0."""
+    ux = np.array([x ** j for j in range(nx)])
+    uy = np.array([y ** j for j in range(ny)])
+    uz = np.array([z ** j for j in range(nz)])
+    Sx, Sy, Sz = ux @ Qx.T, uy @ Qy.T, uz @ Qz.T
+    uxp = np.array([j * x ** (j - 1) if j else 0.0 for j in range(nx)])
+    uyp = np.array([j * y ** (j - 1) if j else 0.0 for j in range(ny)])
+    uzp = np.array([j * z ** (j - 1) if j else 0.0 for j in range(nz)])
+    Sxp, Syp, Szp = Qx @ uxp, uyp @ Qy.T, uzp @ Qz.T
+    n = nx * ny * nz
+    Nx, Ny, Nz = np.zeros(n), np.zeros(n), np.zeros(n)
+    cc = 0
+    for j3 in range(nz):
+        for j2 in range(ny):
+            for j1 in range(nx):
+                a = Sxp[j1] * Sy[j2] * Sz[j3]
+                b = Sx[j1] * Syp[j2] * Sz[j3]
+                c = Sx[j1] * Sy[j2] * Szp[j3]
+                Nx[cc] = 0.0 if abs(a) < 1e-12 else a
+                Ny[cc] = 0.0 if abs(b) < 1e-12 else b
+                Nz[cc] = 0.0 if abs(c) < 1e-12 else c
+                cc += 1
+    return Nx, Ny, Nz
+
+
+def coupl3d_global(epzt, gpzt, x, y, z, Qx, Qy, Qz, ksi, eta, dzeta, wx, wy, wz):
+    """``flat_shell_engine/coupl3D_global.m:1-150``: piezo element matrices
+    kufi [3N x N] and kfifi [N x N] of one 3D spectral element."""
+    nx, ny, nz = len(ksi), len(eta), len(dzeta)
+    N = nx * ny * nz
+    kufi = np.zeros((3 * N, N))
+    kfifi = np.zeros((N, N))
+    for kz in range(nz):
+        for ky in range(ny):
+            for kx in range(nx):
+                Px, Py, Pz = shape3d_prim(nx, ny, nz, Qx, Qy, Qz, ksi[kx], eta[ky], dzeta[kz])
+                J = np.array([[Px @ x, Px @ y, Px @ z], [Py @ x, Py @ y, Py @ z], [Pz @ x, Pz @ y, Pz @ z]])
+                Jj = J.reshape(-1)
+                V3 = np.array([Jj[1] * Jj[5] - Jj[4] * Jj[2], Jj[3] * Jj[2] - Jj[0] * Jj[5], Jj[0] * Jj[4] - Jj[3] * Jj[1]])
+                v3 = V3 / np.sqrt(V3 @ V3)
+                v1 = Jj[:3] / np.sqrt(Jj[:3] @ Jj[:3])
+                v2 = np.array([v3[1] * v1[2] - v3[2] * v1[1], -v3[0] * v1[2] + v3[2] * v1[0], v3[0] * v1[1] - v3[1] * v1[0]])
+                v2 = v2 / np.sqrt(v2 @ v2)
+                inJ = np.linalg.inv(J)
+                detJ = np.linalg.det(J)
+                w = wx[kx] * wy[ky] * wz[kz] * detJ
+                Nxx = Px * inJ[0, 0] + Py * inJ[0, 1] + Pz * inJ[0, 2]
+                Nyy = Px * inJ[1, 0] + Py * inJ[1, 1] + Pz * inJ[1, 2]
+                Nzz = Px * inJ[2, 0] + Py * inJ[2, 1] + Pz * inJ[2, 2]
+                B = np.zeros((6, 3 * N))
+                B[0, 0::3] = Nxx
+                B[1, 1::3] = Nyy
+                B[2, 2::3] = Nzz
+                B[3, 0::3] = Nyy
+                B[3, 1::3] = Nxx
+                B[4, 1::3] = Nzz
+                B[4, 2::3] = Nyy
+                B[5, 0::3] = Nzz
+                B[5, 2::3] = Nxx
+                Bfi = np.stack([Nxx * v1[0] + Nyy * v1[1] + Nzz * v1[2],
+                                Nxx * v2[0] + Nyy * v2[1] + Nzz * v2[2],
+                                Nxx * v3[0] + Nyy * v3[1] + Nzz * v3[2]])
+                kufi += (B.T @ epzt.T @ Bfi) * w
+                kfifi += Bfi.T @ gpzt @ Bfi * w
+    return kufi, kfifi
+
+
+def connect_pzt3d(nx, ny, nz, pztEl0, nodes1, coords, pzt_t, h):
+    """``flat_shell/mesher/connect_pzt3D_to_plate_fun.m`` + ``remove_free_spec_nodes.m``:
+    3D PZT elements on top of the plate elements pztEl0 (0-based); returns
+    nodespzt [npzt, nx*ny*nz] 1-based (compact numbering), coordspzt and the
+    plate node of each compact node (0 if not on the plate)."""
+    ksi, _ = gll(nz)
+    npzt = len(pztEl0)
+    Nodemax = int(nodes1.max())
+    nl = nx * ny
+    nodespzt = np.zeros((npzt, nl * nz), dtype=np.int64)
+    nodespzt[:, :nl] = nodes1[pztEl0, :nl]
+    Bn, J = np.unique(nodespzt[:, :nl].T.reshape(-1), return_inverse=True)  # column-major as in MATLAB
+    doflay = len(Bn)
+    J = J.reshape(nl, npzt).T  # back to [element, node] order
+    for k in range(1, nz):
+        nodespzt[:, nl * k: nl * (k + 1)] = (np.arange(doflay) + 1 + Nodemax)[J]
+        Nodemax += doflay
+    coordspzt = np.zeros((Nodemax + 1, 3))
+    for m in range(npzt):
+        ne = pztEl0[m]
+        for k in range(nz):
+            idx = nodespzt[m, nl * k: nl * (k + 1)]
+            coordspzt[idx, 0] = coords[nodes1[ne] - 1, 0]
+            coordspzt[idx, 1] = coords[nodes1[ne] - 1, 1]
+            coordspzt[idx, 2] = coords[nodes1[ne, :nl] - 1, 2] + (ksi[k] + 1) / 2 * pzt_t + h / 2
+    used = np.unique(nodespzt)
+    nodemap = np.zeros(Nodemax + 1, dtype=np.int64)
+    nodemap[used] = np.arange(1, len(used) + 1)
+    plate_of = np.where(used <= int(nodes1.max()), used, 0)
+    return nodemap[nodespzt], coordspzt[used], plate_of
+
+
+def find_boundary_nodes(nodes1, nx, ny):
+    """``flat_shell/mesher/find_boundary_nodes.m``: nodes on the boundary of
+    the element patch (corners shared by <= 2 elements, edge nodes of one
+    element), in the reference's visiting order (1-based, may repeat)."""
+    fen = nodes1.shape[0]
+    mc = [0, nx - 1, nx * ny - nx, nx * ny - 1]
+    e1 = list(range(1, nx - 1))
+    e2 = [(k + 2) * nx - 1 for k in range(ny - 2)]
+    e3 = list(range(nx * ny - nx + 1, nx * ny - 1))
+    e4 = [(k + 1) * nx for k in range(ny - 2)]
+    out = []
+    for k in range(fen):
+        others = [j for j in range(fen) if j != k]
+        for i in range(4):
+            cn = nodes1[k, mc[i]]
+            nb = sum(1 for j in others for jc in range(4) if nodes1[j, mc[jc]] == cn)
+            if nb <= 1:
+                out.append(cn)
+        for edge in (e1, e2, e3, e4):
+            for i in edge:
+                en = nodes1[k, i]
+                nb = sum(1 for j in others for e in (e1, e2, e3, e4) for jc in e if nodes1[j, jc] == en)
+                if nb == 0:
+                    out.append(en)
+    return np.array(out, dtype=np.int64)
+
+
+def pzt_actuator_forces(nodes1, coords, pztEl0, pzt_t, h, V0, epzt, gpzt, nx=6, ny=6, nz=3):
+    """Equivalent nodal loads Fa [5*nnode] of one PZT actuator driven at V0,
+    ``main_flat_shell.m:144-225`` (bottom electrode 0 V, top V0, internal
+    potential from the static condensation, in-plane forces of the bottom
+    layer taken at the patch boundary, moments with lever h/2 + t/2)."""
+    ksi, wx = gll(nx)
+    eta, wy = gll(ny)
+    dz, wz = gll(nz)
+    Qx, Qy, Qz = vandermonde(ksi), vandermonde(eta), vandermonde(dz)
+    nodespzt, cpzt, plate_of = connect_pzt3d(nx, ny, nz, pztEl0, nodes1, coords, pzt_t, h)
+    nl = nx * ny
+    EBC0 = np.unique(nodespzt[:, :nl])
+    EBCI = np.unique(nodespzt[:, nl:-nl])
+    EBCN = np.unique(nodespzt[:, -nl:])
+    NofNodes = int(nodespzt.max())
+    Kfiu = np.zeros((NofNodes, 3 * NofNodes))
+    Kfifi = np.zeros((NofNodes, NofNodes))
+    for c in range(len(pztEl0)):
+        nd = nodespzt[c] - 1
+        kufi, kfifi = coupl3d_global(epzt, gpzt, cpzt[nd, 0], cpzt[nd, 1], cpzt[nd, 2], Qx, Qy, Qz, ksi, eta, dz,
+                                     wx, wy, wz)
+        dof = (3 * nd[:, None] + np.arange(3)[None, :]).reshape(-1)
+        Kfiu[np.ix_(nd, dof)] += kufi.T
+        Kfifi[np.ix_(nd, nd)] += kfifi
+    I, Nn = EBCI - 1, EBCN - 1
+    Fetemp = Kfifi[np.ix_(I, Nn)] @ np.full(len(Nn), V0)
+    fiAi = -np.linalg.solve(Kfifi[np.ix_(I, I)], Fetemp)
+    FiA = np.zeros(NofNodes)
+    FiA[Nn] = V0
+    FiA[I] = fiAi
+    FaL = Kfiu.T @ FiA
+    bn_pzt = find_boundary_nodes(nodespzt[:, :nl], nx, ny)
+    bn_glob = find_boundary_nodes(nodes1[pztEl0, :nl], nx, ny)
+    nnode = coords.shape[0]
+    FaxG = np.zeros(nnode)
+    FayG = np.zeros(nnode)
+    FaxG[bn_glob - 1] = FaL[0::3][bn_pzt - 1]
+    FayG[bn_glob - 1] = FaL[1::3][bn_pzt - 1]
+    Fa = np.zeros(5 * nnode)
+    Fa[0::5] = FaxG
+    Fa[2::5] = FayG
+    Fa[1::5] = FaxG * (h / 2 + pzt_t / 2)
+    Fa[3::5] = FayG * (h / 2 + pzt_t / 2)
+    return Fa

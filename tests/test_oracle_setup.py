@@ -145,3 +145,21 @@ def test_structured_mesh_and_baskets(pkg):
         assert len(g) == len(np.unique(g))
     assert np.count_nonzero(IL) == 12 * 36
     assert sorted(IL[IL > 0].tolist()) == list(range(1, 12 * 36 + 1))
+
+
+@pytest.mark.parametrize("nex,elems", [(4, [5, 6, 9, 10]), (5, [6, 7, 8, 11, 12, 13]), (3, [4])])
+def test_pzt_actuator_loads_match_reference(pkg, nex, elems):
+    """pzt.actuator_loads (own tensor-product integration) == the literal
+    restatement of main_flat_shell.m:144-225 / coupl3D_global.m; the loads
+    are self-equilibrated."""
+    p = pkg.materials.pzt5a()
+    pc = R.pzt_const(p["S"], p["d"], p["epsT"], 0.0)
+    mp = pkg.materials.pzt_material(p["S"], p["d"], p["epsT"], 0.0)
+    m = pkg.mesh.structured_plate(0.005 * nex, 0.005 * nex, nex, nex)
+    Fo = R.pzt_actuator_forces(m["nodes"], m["coords"], np.array(elems), 0.2e-3, 3.9e-3, 100.0, pc["epzt"],
+                               pc["gpzt"])
+    Fp = pkg.pzt.actuator_loads(m, elems, 0.2e-3, 3.9e-3, 100.0, mp["epzt"], mp["gpzt"])
+    assert np.linalg.norm(Fo) > 0
+    assert np.linalg.norm(Fp - Fo) <= 1e-12 * np.linalg.norm(Fo)
+    assert abs(Fp[0::5].sum()) <= 1e-12 * np.abs(Fp[0::5]).max()
+    assert abs(Fp[2::5].sum()) <= 1e-12 * np.abs(Fp[2::5]).max()
