@@ -219,13 +219,20 @@ def single_plate_bench(pkg, args):
     shm_forward (outputs, PZT voltage, frames), FP32 error vs the FP64 run."""
     import torch
     W = pkg.workloads
-    scs, run = W.plate_force() if args.workload == "force" else W.plate_pzt()
-    ndof = W.dof_count(scs)
+    if args.workload == "solid":
+        scs, run = W.solid_plate()
+        ndof = int(3 * np.asarray(scs[0].mesh["coords"]).shape[0])
+    else:
+        scs, run = W.plate_force() if args.workload == "force" else W.plate_pzt()
+        ndof = W.dof_count(scs)
     nsteps = run.nft - run.nn_first + 1
     res, out = {}, {"workload": args.workload, "dof": ndof, "nft": run.nft, "dt_s": run.dt,
                     "frames": run.frm_int > 0}
     for prec in (64, 32):
-        p = pkg.Plan(scs, run, precision=prec, path=0, steps_per_graph=50)
+        if args.workload == "solid":
+            p = pkg.SolidPlan(scs, run, precision=prec, steps_per_graph=50)
+        else:
+            p = pkg.Plan(scs, run, precision=prec, path=0, steps_per_graph=50)
         if p.info["path"] == 2 and prec == 32:
             out["autotune"] = p.autotune(10)
         p.forward(want_frames=run.frm_int > 0)
@@ -268,7 +275,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adjoint", action="store_true", help="damage-gradient workload instead of the forward batch")
-    ap.add_argument("--workload", choices=("batch", "force", "pzt"), default="batch",
+    ap.add_argument("--workload", choices=("batch", "force", "pzt", "solid"), default="batch",
                     help="batch: 512 plates (default); force: 20x20-element plate; pzt: 200x200 plate with PZT")
     ap.add_argument("--adj-maps", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=20000)

@@ -138,6 +138,36 @@ shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
  * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task. */
 shm_status shm_plan_info(const shm_plan *plan, int64_t *info9);
 
+/* 3D solid (src/models/solid3D/main_spec3Dcuda_global_cpu_gpu3_wave_sens_opt_single_PCT_mat.m):
+ * hexahedral spectral elements of 6 x 6 x 3 nodes, 3 DOF per node (u, v, w;
+ * DOF 3*(node-1)+{1,2,3}).  nodes [fen x 108] column-major, 1-based, local
+ * order x fastest, then y, then z (shape3D_prim_v2.m, extrude_mesh.m). */
+typedef struct {
+  int32_t fen, npe, nnode;
+  const int32_t *nodes;    /* [fen x 108] column-major, 1-based */
+  const double *coords;    /* [nnode x 3] column-major */
+  int32_t basket_rows;
+  const int32_t *I_G, *I_L;
+} shm_solid_mesh;
+
+/* material rows: D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55 D56 D66 rho
+ * (stresses_spec_p.m, Voigt order xx yy zz xy yz xz). */
+#define SHM_SOLID_MAT_STRIDE 14
+typedef struct {
+  int32_t nmat;
+  const double *table;     /* [nmat x 14] row-major */
+  const int32_t *elem_mat; /* [fen] 0-based, NULL = 0 */
+  const double *elem_keep; /* [fen] stiffness factor, NULL = 1 */
+} shm_solid_material;
+
+/* Creates a 3D-solid plan; shm_forward, shm_reset, shm_set_signal,
+ * shm_advance, shm_read_outputs, shm_time_steps, shm_get_state (3 values per
+ * node), shm_set_state, shm_mass and shm_plan_destroy accept it.  shm_run's
+ * force_dof/out_dof use the 3-DOF numbering, frame_dof is 1..3, PZT sensor
+ * fields are ignored. */
+shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh *meshes, const shm_solid_material *mats,
+                                 const shm_run *runs, const shm_options *opt, shm_plan **out);
+
 /* Discrete adjoint of the whole forward solve (no counterpart in the
  * reference, which has no gradients).  Misfit per scenario
  *   J = 1/2 sum_q sum_{nn=nn_first..nft} (displ(nn,q) - target(nn,q))^2

@@ -14,7 +14,8 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libshmsem.so")
 SOURCES = [os.path.join(PKG_DIR, "csrc", f) for f in ("shmsem.cu", "static_stiffness.cu")]
-HEADERS = [os.path.join(PKG_DIR, "csrc", f) for f in ("shell_element.cuh", "shell_structured.cuh")] + [
+HEADERS = [os.path.join(PKG_DIR, "csrc", f) for f in ("shell_element.cuh", "shell_structured.cuh",
+                                                       "shell_structured_f32.cuh", "solid_element.cuh")] + [
     os.path.join(REPO_DIR, "include", "shmsem.h")]
 
 NVCC_FLAGS = [

@@ -316,6 +316,7 @@ __global__ void k_voltage(const double* vsum, const int* sptr, double* volt, int
 // ---------------------------------------------------------------------------
 #include "shell_structured.cuh"
 #include "shell_structured_f32.cuh"
+#include "solid_element.cuh"
 
 // laminate coefficient pairs for the packed FP32 kernel (indices into a table row)
 static const int kLamPairs[LAMP][2] = {{0, 1},   {1, 3},   {2, 4},   {9, 10},  {10, 12}, {11, 13}, {2, 9},
@@ -350,6 +351,8 @@ struct DevBuf {
 
 struct shm_plan {
   std::string err;
+  int kind = 0;  // 0 flat shell (5 DOF/node), 1 3D solid (3 DOF/node)
+  int nf = 5;    // fields (DOF) per node
   int prec = 64, path = 1, device = 0, steps_per_graph = 0, tile = 0;
   cudaStream_t stream = nullptr;
   int nscen = 0;
@@ -618,7 +621,11 @@ static cudaError_t launch_general_step(shm_plan* p, int kstep, cudaStream_t s) {
 
 template <typename T> static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s);
 
+template <typename T> static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s);
+
 static cudaError_t launch_step(shm_plan* p, int kstep, cudaStream_t s) {
+  if (p->kind == 1)
+    return p->prec == 64 ? launch_solid_step<double>(p, kstep, s) : launch_solid_step<float>(p, kstep, s);
   if (p->path == 2) {
     return p->prec == 64 ? launch_struct_step<double>(p, kstep, s) : launch_struct_step<float>(p, kstep, s);
   }
@@ -1357,8 +1364,8 @@ extern "C" shm_status shm_reset(shm_plan* p) {
   if (!p) return SHM_ERR_BAD_ARG;
   cudaStream_t s = p->stream;
   const size_t ts = p->prec == 64 ? 8 : 4;
-  CKP(p, cudaMemsetAsync(p->UA, 0, ts * 5 * p->nnode_pad, s));
-  CKP(p, cudaMemsetAsync(p->UB, 0, ts * 5 * p->nnode_pad, s));
+  CKP(p, cudaMemsetAsync(p->UA, 0, ts * p->nf * p->nnode_pad, s));
+  CKP(p, cudaMemsetAsync(p->UB, 0, ts * p->nf * p->nnode_pad, s));
   if (p->frames) CKP(p, cudaMemsetAsync(p->frames, 0, ts * p->nframes * p->nnode_pad, s));
   CKP(p, cudaMemsetAsync(p->displ, 0, sizeof(double) * std::max(p->nout, 1) * p->nft, s));
   CKP(p, cudaMemsetAsync(p->vsum, 0, sizeof(double) * std::max(p->nslot, 1) * p->nft, s));
@@ -1519,14 +1526,15 @@ extern "C" shm_status shm_forward(shm_plan* p, const double* st, double* displ, 
 template <typename T>
 static shm_status get_state_t(shm_plan* p, double* U, double* uold) {
   const bool odd = ((p->nn - p->nn_first) & 1);
-  std::vector<T> h((size_t)5 * p->nnode_pad);
+  const int nf = p->nf;
+  std::vector<T> h((size_t)nf * p->nnode_pad);
   for (int which = 0; which < 2; ++which) {
     double* out = which == 0 ? U : uold;
     if (!out) continue;
     const void* src = (which == 0) ? (odd ? p->UB : p->UA) : (odd ? p->UA : p->UB);
     CKP(p, cudaMemcpy(h.data(), src, sizeof(T) * h.size(), cudaMemcpyDeviceToHost));
     for (int64_t g = 0; g < p->nnode; ++g)
-      for (int f = 0; f < 5; ++f) out[5 * g + f] = (double)h[(size_t)f * p->nnode_pad + g];
+      for (int f = 0; f < nf; ++f) out[nf * g + f] = (double)h[(size_t)f * p->nnode_pad + g];
   }
   return SHM_OK;
 }
@@ -1536,13 +1544,14 @@ static shm_status set_state_t(shm_plan* p, const double* U, const double* uold, 
   p->nn = nn;
   CKP(p, cudaMemcpy(p->d_base, &nn, 4, cudaMemcpyHostToDevice));
   const bool odd = ((nn - p->nn_first) & 1);
-  std::vector<T> h((size_t)5 * p->nnode_pad, T(0));
+  const int nf = p->nf;
+  std::vector<T> h((size_t)nf * p->nnode_pad, T(0));
   for (int which = 0; which < 2; ++which) {
     const double* in = which == 0 ? U : uold;
     std::fill(h.begin(), h.end(), T(0));
     if (in)
       for (int64_t g = 0; g < p->nnode; ++g)
-        for (int f = 0; f < 5; ++f) h[(size_t)f * p->nnode_pad + g] = (T)in[5 * g + f];
+        for (int f = 0; f < nf; ++f) h[(size_t)f * p->nnode_pad + g] = (T)in[nf * g + f];
     void* dst = (which == 0) ? (odd ? p->UB : p->UA) : (odd ? p->UA : p->UB);
     CKP(p, cudaMemcpy(dst, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
   }
@@ -1598,6 +1607,7 @@ static shm_status apply_k_t(shm_plan* p, const double* U, double* F) {
 
 extern "C" shm_status shm_apply_stiffness(shm_plan* p, const double* U, double* F) {
   if (!p || !U || !F) return SHM_ERR_BAD_ARG;
+  if (p->kind != 0) return bad(p, "apply_stiffness: flat-shell plans only");
   CKP(p, cudaStreamSynchronize(p->stream));
   return p->prec == 64 ? apply_k_t<double>(p, U, F) : apply_k_t<float>(p, U, F);
 }
@@ -1606,7 +1616,7 @@ extern "C" shm_status shm_plan_info(const shm_plan* p, int64_t* info) {
   if (!p || !info) return SHM_ERR_BAD_ARG;
   info[0] = p->nnode;
   info[1] = p->fen;
-  info[2] = 5 * p->nnode;
+  info[2] = (int64_t)p->nf * p->nnode;
   info[3] = p->path;
   info[4] = p->prec;
   info[5] = p->nframes;
@@ -1813,9 +1823,327 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
 extern "C" shm_status shm_forward_backward(shm_plan* p, const double* st, const double* target, double* misfit,
                                            double* grad, int32_t ckpt_every, void* stream) {
   if (!p || !st || !target) return SHM_ERR_BAD_ARG;
+  if (p->kind != 0) return bad(p, "forward_backward: flat-shell plans only");
   if (p->nout < 1) return bad(p, "forward_backward: the misfit needs point outputs");
   cudaStream_t s = pick_stream(p, stream);
   drop_graph(p);
   return p->prec == 64 ? fwd_bwd_t<double>(p, st, target, misfit, grad, ckpt_every, s)
                        : fwd_bwd_t<float>(p, st, target, misfit, grad, ckpt_every, s);
+}
+
+// ---------------------------------------------------------------------------
+// 3D solid plans (6x6x3 hexahedra, 3 DOF per node)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
+  SolidArgs<T> a;
+  a.fen_pad = p->fen_pad;
+  a.nnode_pad = p->nnode_pad;
+  a.plane = p->plane;
+  a.nnode = (int)p->nnode;
+  a.fen = (int)p->fen;
+  a.nn_first = p->nn_first;
+  a.nft = p->nft;
+  a.UA = (T*)p->UA;
+  a.UB = (T*)p->UB;
+  a.F2 = (T*)p->F2;
+  a.conn = p->conn;
+  a.geo = (const T*)p->geo;
+  a.emat = p->emat;
+  a.ekeep = (const T*)p->ekeep;
+  a.mat = (const T*)p->mat;
+  a.row_ptr = p->row_ptr;
+  a.slots = p->slots;
+  a.minv = (const T*)p->minv;
+  for (int f = 0; f < 3; ++f) {
+    a.k1[f] = (T)p->k1[f];
+    a.k2[f] = (T)p->k2[f];
+  }
+  a.nforce = p->nforce;
+  a.fq_field = p->fq_field;
+  a.fq_scen = p->fq_scen;
+  a.fq_val = p->fq_val;
+  a.st = p->st;
+  a.nout = p->nout;
+  a.out_node = p->out_node;
+  a.out_field = p->out_field;
+  a.displ = p->displ;
+  a.frm_int = p->frm_int;
+  a.frame_field = p->frame_field;
+  a.nframes = p->nframes;
+  a.frames = (T*)p->frames;
+  a.a1 = (T)p->a1;
+  a.blowup = (T)p->blowup;
+  a.flag = p->flag;
+  a.d_base = p->d_base;
+  k_elem_solid<T><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
+  k_node_solid<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kstep);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const std::vector<double>& geo,
+                               const std::vector<int>& emat, const std::vector<double>& ekeep,
+                               const std::vector<double>& mat, const std::vector<double>& minv) {
+  auto conv = [](const std::vector<double>& v) {
+    std::vector<T> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) o[i] = (T)v[i];
+    return o;
+  };
+  shm_status s;
+  T *g = nullptr, *k = nullptr, *m = nullptr, *mi = nullptr, *ua = nullptr, *ub = nullptr, *f2 = nullptr,
+    *fr = nullptr;
+  if ((s = upload(p, &p->conn, conn)) != SHM_OK) return s;
+  if ((s = upload(p, &g, conv(geo))) != SHM_OK) return s;
+  if ((s = upload(p, &p->emat, emat)) != SHM_OK) return s;
+  if ((s = upload(p, &k, conv(ekeep))) != SHM_OK) return s;
+  if ((s = upload(p, &m, conv(mat))) != SHM_OK) return s;
+  if ((s = upload(p, &mi, conv(minv))) != SHM_OK) return s;
+  if ((s = dalloc(p, &ua, (size_t)3 * p->nnode_pad)) != SHM_OK) return s;
+  if ((s = dalloc(p, &ub, (size_t)3 * p->nnode_pad)) != SHM_OK) return s;
+  if ((s = dalloc(p, &f2, (size_t)3 * p->plane)) != SHM_OK) return s;
+  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nnode_pad)) != SHM_OK) return s;
+  p->geo = g;
+  p->ekeep = k;
+  p->mat = m;
+  p->minv = mi;
+  p->UA = ua;
+  p->UB = ub;
+  p->F2 = f2;
+  p->frames = fr;
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh* meshes,
+                                            const shm_solid_material* mats, const shm_run* runs,
+                                            const shm_options* opt, shm_plan** out) {
+  if (!out) return SHM_ERR_BAD_ARG;
+  *out = nullptr;
+  if (nscen < 1 || !meshes || !mats || !runs) return SHM_ERR_BAD_ARG;
+  shm_plan* p = new shm_plan();
+  *out = p;
+  p->kind = 1;
+  p->nf = 3;
+  shm_options o{};
+  o.precision = 64;
+  if (opt) o = *opt;
+  if (o.precision != 64 && o.precision != 32) return bad(p, "precision must be 32 or 64");
+  p->prec = o.precision;
+  p->device = o.device;
+  p->steps_per_graph = std::max(0, o.steps_per_graph);
+  p->nscen = nscen;
+  p->path = 1;
+  CKP(p, cudaSetDevice(o.device));
+  CKP(p, cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  const shm_run& r0 = runs[0];
+  if (!(r0.dt > 0) || r0.nft < 1 || (r0.nn_first != 1 && r0.nn_first != 2))
+    return bad(p, "run: dt > 0, nft >= 1, nn_first in {1,2} required");
+  for (int s = 1; s < nscen; ++s)
+    if (runs[s].dt != r0.dt || runs[s].nft != r0.nft || runs[s].nn_first != r0.nn_first ||
+        runs[s].eta_xy != r0.eta_xy || runs[s].eta_z != r0.eta_z || runs[s].frm_int != r0.frm_int)
+      return bad(p, "all scenarios of a batch must share dt, nft, nn_first, damping and frames");
+  p->dt = r0.dt;
+  p->nft = r0.nft;
+  p->nn_first = p->nn = r0.nn_first;
+  p->a0 = 1.0 / (r0.dt * r0.dt);
+  p->a1 = 1.0 / (2.0 * r0.dt);
+  // damping: dv(x,y) = etad_xy, dv(z) = etad_z (main_spec3Dcuda_global_...:864-867)
+  const double eta[3] = {r0.eta_xy, r0.eta_xy, r0.eta_z};
+  for (int f = 0; f < 3; ++f) {
+    const double den = p->a0 + p->a1 * eta[f];
+    p->k1[f] = (p->a0 - p->a1 * eta[f]) / den;
+    p->k2[f] = 1.0 / den;
+  }
+  p->frm_int = r0.frm_int > 0 ? r0.frm_int : 0;
+  if (p->frm_int > 0) {
+    if (r0.frame_dof < 1 || r0.frame_dof > 3) return bad(p, "frame_dof must be 1..3 for solids");
+    p->frame_field = r0.frame_dof - 1;
+    p->nframes = r0.nft / p->frm_int;
+  }
+  p->blowup = INFINITY;
+  p->node_off.assign(nscen + 1, 0);
+  p->elem_off.assign(nscen + 1, 0);
+  for (int s = 0; s < nscen; ++s) {
+    const shm_solid_mesh& m = meshes[s];
+    if (m.npe != S_NPE) return bad(p, "solid npe must be 108 (6x6x3)");
+    if (m.fen < 1 || m.nnode < 1 || !m.nodes || !m.coords) return bad(p, "mesh: empty or NULL arrays");
+    p->node_off[s + 1] = p->node_off[s] + m.nnode;
+    p->elem_off[s + 1] = p->elem_off[s] + m.fen;
+  }
+  p->nnode = p->node_off[nscen];
+  p->fen = p->elem_off[nscen];
+  if (p->nnode > INT32_MAX / 2 || p->fen * (int64_t)S_NPE > INT32_MAX / 2) return bad(p, "mesh too large");
+  p->fen_pad = (p->fen + S_EPB - 1) / S_EPB * S_EPB;
+  p->nnode_pad = (p->nnode + 31) / 32 * 32;
+  std::vector<double> gx, gw, D, gx3, gw3, D3;
+  gll_setup(NP, gx, gw, D);
+  gll_setup(S_NZ, gx3, gw3, D3);
+  {
+    float D32[36], D332[9];
+    for (int i = 0; i < 36; ++i) D32[i] = (float)D[i];
+    for (int i = 0; i < 9; ++i) D332[i] = (float)D3[i];
+    CKP(p, cudaMemcpyToSymbol(c_D64, D.data(), sizeof(double) * 36));
+    CKP(p, cudaMemcpyToSymbol(c_D32, D32, sizeof(float) * 36));
+    CKP(p, cudaMemcpyToSymbol(c_D3_64, D3.data(), sizeof(double) * 9));
+    CKP(p, cudaMemcpyToSymbol(c_D3_32, D332, sizeof(float) * 9));
+  }
+  const int64_t FP = p->fen_pad;
+  std::vector<int> conn((size_t)S_NPE * FP, 0), emat(FP, 0);
+  std::vector<double> geo((size_t)10 * S_NPE * FP, 0.0), ekeep(FP, 1.0), mat, erho(FP, 0.0);
+  std::vector<int> node_cnt(p->nnode, 0);
+  int mat_base = 0, nforce_tot = 0;
+  for (int s = 0; s < nscen; ++s) {
+    const shm_solid_mesh& m = meshes[s];
+    for (int c = 0; c < S_NPE; ++c)
+      for (int e = 0; e < m.fen; ++e) {
+        const int nd = m.nodes[(int64_t)c * m.fen + e];
+        if (nd < 1 || nd > m.nnode) return bad(p, "mesh: node number out of range");
+        node_cnt[p->node_off[s] + nd - 1]++;
+      }
+    for (int q = 0; q < runs[s].n_force; ++q) {
+      const int d = runs[s].force_dof[q];
+      if (d < 1 || d > 3 * m.nnode) return bad(p, "run: force DOF out of range");
+      node_cnt[p->node_off[s] + (d - 1) / 3]++;
+    }
+    nforce_tot += runs[s].n_force;
+  }
+  p->nforce = nforce_tot;
+  std::vector<int> row_ptr(p->nnode + 1, 0);
+  for (int64_t g = 0; g < p->nnode; ++g) row_ptr[g + 1] = row_ptr[g] + node_cnt[g];
+  std::vector<int> slots(row_ptr[p->nnode]), fillc(p->nnode, 0);
+  const int64_t P0 = (int64_t)S_NPE * FP;
+  p->plane = (P0 + std::max(nforce_tot, 1) + 31) / 32 * 32;
+  std::vector<int> fq_field, fq_scen, out_node, out_field;
+  std::vector<double> fq_val;
+  int fq = 0;
+  p->out_off.assign(nscen + 1, 0);
+  for (int s = 0; s < nscen; ++s) {
+    const shm_solid_mesh& m = meshes[s];
+    const shm_solid_material& mt = mats[s];
+    const int64_t e0 = p->elem_off[s], n0 = p->node_off[s];
+    if (mt.nmat < 1 || !mt.table) return bad(p, "material: empty table");
+    for (int q = 0; q < mt.nmat; ++q) {
+      for (int k = 0; k < S_MAT; ++k) mat.push_back(mt.table[(int64_t)q * S_MAT + k]);
+      mat.push_back(0.0);
+      mat.push_back(0.0);
+    }
+    for (int e = 0; e < m.fen; ++e) {
+      const int mi = mt.elem_mat ? mt.elem_mat[e] : 0;
+      if (mi < 0 || mi >= mt.nmat) return bad(p, "material: elem_mat out of range");
+      emat[e0 + e] = mat_base + mi;
+      ekeep[e0 + e] = mt.elem_keep ? mt.elem_keep[e] : 1.0;
+      erho[e0 + e] = mt.table[(int64_t)mi * S_MAT + 13];
+    }
+    mat_base += mt.nmat;
+    // geometry at the GLL nodes: J[b][a] = dx_b/dxi_a, invJ = J^-1 (iJ[a][b] = dxi_a/dx_b)
+    for (int e = 0; e < m.fen; ++e) {
+      double X[S_NPE][3];
+      for (int c = 0; c < S_NPE; ++c) {
+        const int nd = m.nodes[(int64_t)c * m.fen + e];
+        conn[(int64_t)c * FP + e0 + e] = (int)(n0 + nd - 1);
+        for (int b = 0; b < 3; ++b) X[c][b] = m.coords[(int64_t)b * m.nnode + nd - 1];
+      }
+      for (int c = 0; c < S_NPE; ++c) {
+        const int cx = c % NP, cy = (c / NP) % NP, cz = c / 36;
+        double J[3][3] = {{0}};  // J[b][a]
+        for (int b = 0; b < 3; ++b) {
+          for (int q = 0; q < NP; ++q) {
+            J[b][0] += D[cx * NP + q] * X[cz * 36 + cy * NP + q][b];
+            J[b][1] += D[cy * NP + q] * X[cz * 36 + q * NP + cx][b];
+          }
+          for (int q = 0; q < S_NZ; ++q) J[b][2] += D3[cz * S_NZ + q] * X[q * 36 + cy * NP + cx][b];
+        }
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        if (!(std::fabs(det) > 0)) return bad(p, "mesh: singular solid element " + std::to_string(e + 1));
+        // inverse of J (row b, column a): inv[a][b]
+        double inv[3][3];
+        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        const int64_t base = (int64_t)c * FP + e0 + e;
+        for (int q = 0; q < 9; ++q) geo[(int64_t)q * S_NPE * FP + base] = inv[q / 3][q % 3];
+        geo[(int64_t)9 * S_NPE * FP + base] = gw[cx] * gw[cy] * gw3[cz] * std::fabs(det);
+      }
+    }
+    std::vector<int> IG, IL;
+    int rows = 0;
+    if (m.basket_rows > 0 && m.I_G && m.I_L) {
+      rows = m.basket_rows;
+      IG.assign(m.I_G, m.I_G + (size_t)rows * 12);
+      IL.assign(m.I_L, m.I_L + (size_t)rows * 12);
+    } else {
+      build_baskets(m.fen, S_NPE, m.nnode, m.nodes, IG, IL, rows);
+    }
+    for (int b = 0; b < 12; ++b)
+      for (int r = 0; r < rows; ++r) {
+        const int kg = IG[(size_t)b * rows + r], kl = IL[(size_t)b * rows + r];
+        if (kg == 0) continue;
+        if (kg < 1 || kg > m.nnode || kl < 1 || kl > m.fen * S_NPE) return bad(p, "mesh: basket map out of range");
+        const int e = (kl - 1) / S_NPE, c = (kl - 1) % S_NPE;
+        const int64_t g = n0 + kg - 1;
+        if (fillc[g] >= node_cnt[g]) return bad(p, "mesh: basket maps inconsistent with nodes");
+        slots[row_ptr[g] + fillc[g]++] = (int)(c * FP + e0 + e);
+      }
+    for (int q = 0; q < runs[s].n_force; ++q) {
+      const int d = runs[s].force_dof[q];
+      const int64_t g = n0 + (d - 1) / 3;
+      slots[row_ptr[g] + fillc[g]++] = (int)(P0 + fq);
+      fq_field.push_back((d - 1) % 3);
+      fq_scen.push_back(s);
+      fq_val.push_back(runs[s].force_val[q]);
+      ++fq;
+    }
+    for (int q = 0; q < runs[s].n_out; ++q) {
+      const int d = runs[s].out_dof[q];
+      if (d < 1 || d > 3 * m.nnode) return bad(p, "run: output DOF out of range");
+      out_node.push_back((int)(n0 + (d - 1) / 3));
+      out_field.push_back((d - 1) % 3);
+    }
+    p->out_off[s + 1] = p->out_off[s] + runs[s].n_out;
+  }
+  for (int64_t g = 0; g < p->nnode; ++g)
+    if (fillc[g] != node_cnt[g]) return bad(p, "mesh: basket maps do not cover every element node");
+  p->nout = p->out_off[nscen];
+  p->sens_off.assign(nscen + 1, 0);
+  // lumped mass rho * w * detJ (mass3D_v2.m), summed in basket order
+  std::vector<double> minv((size_t)p->nnode_pad, 0.0);
+  p->mass.assign((size_t)3 * p->nnode, 0.0);
+  for (int64_t g = 0; g < p->nnode; ++g) {
+    double mm = 0.0;
+    for (int q = row_ptr[g]; q < row_ptr[g + 1]; ++q) {
+      const int64_t sl = slots[q];
+      if (sl >= P0) continue;
+      const int64_t c = sl / FP, e = sl % FP;
+      mm += geo[(int64_t)9 * S_NPE * FP + c * FP + e] * erho[e];
+    }
+    minv[g] = mm > 0 ? 1.0 / mm : 0.0;
+    for (int f = 0; f < 3; ++f) p->mass[3 * g + f] = mm;
+  }
+  shm_status st = p->prec == 64 ? solid_device<double>(p, conn, geo, emat, ekeep, mat, minv)
+                                : solid_device<float>(p, conn, geo, emat, ekeep, mat, minv);
+  if (st != SHM_OK) return st;
+  if ((st = upload(p, &p->row_ptr, row_ptr)) != SHM_OK) return st;
+  if ((st = upload(p, &p->slots, slots)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_field, fq_field)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_scen, fq_scen)) != SHM_OK) return st;
+  if ((st = upload(p, &p->fq_val, fq_val)) != SHM_OK) return st;
+  if ((st = upload(p, &p->out_node, out_node)) != SHM_OK) return st;
+  if ((st = upload(p, &p->out_field, out_field)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->st, (size_t)nscen * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->displ, (size_t)std::max(p->nout, 1) * p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->vsum, (size_t)p->nft)) != SHM_OK) return st;  // cleared by shm_reset
+  if ((st = dalloc(p, &p->volt, (size_t)p->nft)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->flag, 4)) != SHM_OK) return st;
+  if ((st = dalloc(p, &p->d_base, 4)) != SHM_OK) return st;
+  CKP(p, cudaDeviceSynchronize());
+  return shm_reset(p);
 }

@@ -1,0 +1,187 @@
+// 3D solid spectral element: 6 x 6 x 3 GLL nodes (order 5 in plane, order 2
+// through the ply), 3 DOF per node (u, v, w), general hexahedral geometry.
+//
+// Restates the per-step work of the reference's 3D solver
+// (src/models/solid3D/main_spec3Dcuda_global_cpu_gpu3_wave_sens_opt_single_PCT_mat.m:922-1010):
+//   strains_spec_p.m   Exx..Exz from the 9 derivative products,
+//   stresses_spec_p.m  Sxx..Sxz = D * E with D11..D66 (Voigt xx yy zz xy yz xz),
+//   forces             fu, fv, fw = sum of 27 transposed products (:944-954),
+// as one kernel: a thread per element node, the element's displacements and
+// weighted fluxes staged in shared memory, the three 1D derivative matrices
+// (6-point along xi and eta, 3-point along zeta) applied by each thread along
+// its own node lines.  Element-local forces go to scratch and are assembled by
+// the node kernel exactly like the flat shell's general path.
+#pragma once
+#include "shell_element.cuh"
+
+namespace shm {
+
+constexpr int S_NZ = 3;
+constexpr int S_NPE = NP * NP * S_NZ;   // 108 nodes per element
+constexpr int S_EPB = 2;                // elements per CTA
+constexpr int S_THREADS = S_NPE * S_EPB;
+constexpr int S_MAT = 14;               // D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55 D56 D66 rho
+constexpr int S_MAT_DEV = 16;
+
+static __constant__ double c_D3_64[S_NZ * S_NZ];
+static __constant__ float c_D3_32[S_NZ * S_NZ];
+template <typename T> __device__ __forceinline__ T D3m(int r, int c);
+template <> __device__ __forceinline__ double D3m<double>(int r, int c) { return c_D3_64[r * S_NZ + c]; }
+template <> __device__ __forceinline__ float D3m<float>(int r, int c) { return c_D3_32[r * S_NZ + c]; }
+
+template <typename T> struct SolidArgs {
+  int64_t fen_pad, nnode_pad, plane;
+  int nnode, fen, nn_first, nft;
+  T* UA;
+  T* UB;
+  T* F2;                           // [3][plane], element slots c*fen_pad + e, then force slots
+  const int* __restrict__ conn;    // [108][fen_pad]
+  const T* __restrict__ geo;       // [10][108][fen_pad]: invJ_ab (a = xi,eta,zeta; b = x,y,z) row-major, W
+  const int* __restrict__ emat;
+  const T* __restrict__ ekeep;
+  const T* __restrict__ mat;       // [nmat][16]
+  const int* __restrict__ row_ptr;
+  const int* __restrict__ slots;
+  const T* __restrict__ minv;      // [nnode_pad]
+  T k1[3], k2[3];
+  int nforce;
+  const int* __restrict__ fq_field;
+  const int* __restrict__ fq_scen;
+  const double* __restrict__ fq_val;
+  const double* __restrict__ st;
+  int nout;
+  const int* __restrict__ out_node;
+  const int* __restrict__ out_field;
+  double* displ;
+  int frm_int, frame_field, nframes;
+  T* frames;
+  T a1, blowup;
+  int* flag;
+  const int* d_base;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int kstep) {
+  __shared__ T su[S_EPB][3][S_NPE];
+  __shared__ T sg[S_EPB][9][S_NPE];   // flux of field f along direction d at [f*3+d]
+  const int nn = *a.d_base + kstep;
+  const T* __restrict__ cur = ((nn - a.nn_first) & 1) ? a.UB : a.UA;
+  if (blockIdx.x == 0) {
+    const int64_t p0 = (int64_t)S_NPE * a.fen_pad;
+    for (int q = threadIdx.x; q < a.nforce; q += blockDim.x) {
+      const double s = a.st[(int64_t)a.fq_scen[q] * a.nft + (nn - 1)];
+      const T val = (T)(-a.fq_val[q] * s);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) a.F2[f * a.plane + p0 + q] = (f == a.fq_field[q]) ? val : T(0);
+    }
+    for (int q = threadIdx.x; q < a.nout; q += blockDim.x)
+      a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
+  }
+  const int le = threadIdx.x / S_NPE;
+  const int c = threadIdx.x % S_NPE;
+  const int e = blockIdx.x * S_EPB + le;
+  const int cx = c % NP, cy = (c / NP) % NP, cz = c / (NP * NP);
+  const int node = a.conn[(int64_t)c * a.fen_pad + e];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) su[le][f][c] = cur[f * a.nnode_pad + node];
+  __syncthreads();
+  // reference derivatives (Npx*U, Npy*U, Npz*U)
+  T d[3][3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    T sx = T(0), sy = T(0), sz = T(0);
+#pragma unroll
+    for (int m = 0; m < NP; ++m) {
+      sx = fma(Dm<T>(cx, m), su[le][f][cz * 36 + cy * NP + m], sx);
+      sy = fma(Dm<T>(cy, m), su[le][f][cz * 36 + m * NP + cx], sy);
+    }
+#pragma unroll
+    for (int m = 0; m < S_NZ; ++m) sz = fma(D3m<T>(cz, m), su[le][f][m * 36 + cy * NP + cx], sz);
+    d[f][0] = sx;
+    d[f][1] = sy;
+    d[f][2] = sz;
+  }
+  T iJ[3][3];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * S_NPE + c) * a.fen_pad + e];
+  const T W = a.geo[((int64_t)9 * S_NPE + c) * a.fen_pad + e];
+  // physical gradient g[f][b] = sum_a d[f][a] * invJ_ab  (strains_spec_p.m)
+  T g[3][3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g[f][b] = d[f][0] * iJ[0][b] + d[f][1] * iJ[1][b] + d[f][2] * iJ[2][b];
+  const T Exx = g[0][0], Eyy = g[1][1], Ezz = g[2][2];
+  const T Exy = g[0][1] + g[1][0];
+  const T Eyz = g[1][2] + g[2][1];
+  const T Exz = g[0][2] + g[2][0];
+  const T* __restrict__ Dm_ = a.mat + (int64_t)a.emat[e] * S_MAT_DEV;
+  const T kp = a.ekeep[e];
+  const T D11 = Dm_[0] * kp, D12 = Dm_[1] * kp, D13 = Dm_[2] * kp, D14 = Dm_[3] * kp, D22 = Dm_[4] * kp;
+  const T D23 = Dm_[5] * kp, D24 = Dm_[6] * kp, D33 = Dm_[7] * kp, D34 = Dm_[8] * kp, D44 = Dm_[9] * kp;
+  const T D55 = Dm_[10] * kp, D56 = Dm_[11] * kp, D66 = Dm_[12] * kp;
+  // stresses_spec_p.m
+  const T Sxx = Exx * D11 + Eyy * D12 + Ezz * D13 + Exy * D14;
+  const T Syy = Exx * D12 + Eyy * D22 + Ezz * D23 + Exy * D24;
+  const T Szz = Exx * D13 + Eyy * D23 + Ezz * D33 + Exy * D34;
+  const T Sxy = Exx * D14 + Eyy * D24 + Ezz * D34 + Exy * D44;
+  const T Syz = Eyz * D55 + Exz * D56;
+  const T Sxz = Eyz * D56 + Exz * D66;
+  // fluxes: field u uses (Sxx, Sxy, Sxz), v (Sxy, Syy, Syz), w (Sxz, Syz, Szz)
+  const T S[3][3] = {{Sxx, Sxy, Sxz}, {Sxy, Syy, Syz}, {Sxz, Syz, Szz}};
+#pragma unroll
+  for (int f = 0; f < 3; ++f)
+#pragma unroll
+    for (int aa = 0; aa < 3; ++aa)
+      sg[le][f * 3 + aa][c] = W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
+  __syncthreads();
+  // transposed operators: Npx' (xi), Npy' (eta), Npz' (zeta)
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    T s = T(0);
+#pragma unroll
+    for (int m = 0; m < NP; ++m) {
+      s = fma(Dm<T>(m, cx), sg[le][f * 3 + 0][cz * 36 + cy * NP + m], s);
+      s = fma(Dm<T>(m, cy), sg[le][f * 3 + 1][cz * 36 + m * NP + cx], s);
+    }
+#pragma unroll
+    for (int m = 0; m < S_NZ; ++m) s = fma(D3m<T>(m, cz), sg[le][f * 3 + 2][m * 36 + cy * NP + cx], s);
+    a.F2[f * a.plane + (int64_t)c * a.fen_pad + e] = s;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
+  const int nn = *a.d_base + kstep;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.nnode) return;
+  const bool odd = ((nn - a.nn_first) & 1);
+  const T* __restrict__ cur = odd ? a.UB : a.UA;
+  T* prev = odd ? a.UA : a.UB;
+  T F[3] = {T(0), T(0), T(0)};
+  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
+  const T im = a.minv[g];
+  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  bool bad = false;
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const T u = cur[f * a.nnode_pad + g];
+    const T uo = prev[f * a.nnode_pad + g];
+    const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
+    prev[f * a.nnode_pad + g] = un;
+    if (frame) {
+      if (f == a.frame_field) {
+        const int fc = nn / a.frm_int - 1;
+        if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + g] = a.a1 * (un - uo);
+      }
+      if (!isfinite(un)) bad = true;
+    }
+  }
+  if (bad) atomicOr(a.flag, 1);
+}
+
+}  // namespace shm

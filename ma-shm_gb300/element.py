@@ -124,3 +124,43 @@ def stable_dt(xy_list, lam_list, safety: float = 0.9, order: int = 5) -> float:
     """safety * 2/sqrt(max over elements of lambda_max(M_e^-1 K_e))."""
     lmax = max(max_eigenvalue(xy, lam, order) for xy in xy_list for lam in lam_list)
     return safety * 2.0 / np.sqrt(lmax)
+
+
+def solid_element_matrices(xyz: np.ndarray, drow: np.ndarray, order: int = 5, nz: int = 3):
+    """Dense stiffness (3*N square, DOF order u v w per node) and lumped mass
+    of a 3D solid element with nodes xyz [N, 3] (x fastest, then y, then z),
+    material row (D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55 D56 D66 rho)."""
+    n = order + 1
+    _, w, D = gll_derivative_matrix(n)
+    _, w3, D3 = gll_derivative_matrix(nz)
+    I6, I3 = np.eye(n), np.eye(nz)
+    ops = [np.kron(I3, np.kron(I6, D)), np.kron(I3, np.kron(D, I6)), np.kron(D3, np.kron(I6, I6))]
+    W = np.kron(w3, np.kron(w, w))
+    N = n * n * nz
+    J = np.stack([np.stack([op @ xyz[:, b] for op in ops], -1) for b in range(3)], axis=1)  # [q, b, a]
+    det = np.linalg.det(J)
+    inv = np.linalg.inv(J)                                  # [q, a, b] = dxi_a / dx_b
+    dN = np.stack(ops, axis=1)                              # [q, a, node]
+    grad = np.einsum("qab,qan->qbn", inv, dN)               # [q, b, node]
+    d = drow
+    Dm = np.array([[d[0], d[1], d[2], d[3], 0, 0], [d[1], d[4], d[5], d[6], 0, 0], [d[2], d[5], d[7], d[8], 0, 0],
+                   [d[3], d[6], d[8], d[9], 0, 0], [0, 0, 0, 0, d[10], d[11]], [0, 0, 0, 0, d[11], d[12]]])
+    B = np.zeros((N, 6, 3 * N))
+    gx, gy, gz = grad[:, 0], grad[:, 1], grad[:, 2]
+    B[:, 0, 0::3], B[:, 1, 1::3], B[:, 2, 2::3] = gx, gy, gz
+    B[:, 3, 0::3], B[:, 3, 1::3] = gy, gx          # xy
+    B[:, 4, 1::3], B[:, 4, 2::3] = gz, gy          # yz
+    B[:, 5, 0::3], B[:, 5, 2::3] = gz, gx          # xz
+    DB = np.einsum("st,qtj->qsj", Dm, B, optimize=True)
+    K = np.einsum("qsi,qsj->ij", B * (W * np.abs(det))[:, None, None], DB, optimize=True)
+    m = np.repeat(W * np.abs(det) * d[13], 3)
+    return K, m
+
+
+def solid_stable_dt(xyz: np.ndarray, drows, safety: float = 0.9) -> float:
+    lmax = 0.0
+    for drow in drows:
+        K, m = solid_element_matrices(xyz, np.asarray(drow, float))
+        s = 1.0 / np.sqrt(m)
+        lmax = max(lmax, float(sla.eigvalsh(s[:, None] * K * s[None, :])[-1]))
+    return safety * 2.0 / np.sqrt(lmax)

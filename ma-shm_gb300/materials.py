@@ -191,3 +191,43 @@ def pzt5a():
     eps0 = 8.854e-12
     epsT = np.diag([1730 * eps0, 1730 * eps0, 1700 * eps0])
     return dict(S=S, d=d, epsT=epsT, rho=7750.0)
+
+
+def ply_c3d_rotated(C: np.ndarray, angle_deg: float) -> np.ndarray:
+    """3D ply stiffness (Voigt x y z yz xz xy) rotated about z by the ply angle:
+    Cbar = T^-1 C T^-T with the stress transformation T (Bond matrix)."""
+    t = np.deg2rad(angle_deg)
+    m, n = np.cos(t), np.sin(t)
+    T = np.array([[m * m, n * n, 0, 0, 0, 2 * m * n],
+                  [n * n, m * m, 0, 0, 0, -2 * m * n],
+                  [0, 0, 1, 0, 0, 0],
+                  [0, 0, 0, m, -n, 0],
+                  [0, 0, 0, n, m, 0],
+                  [-m * n, m * n, 0, 0, 0, m * m - n * n]])
+    Ti = np.linalg.inv(T)
+    return Ti @ C @ Ti.T
+
+
+def solid_row(C: np.ndarray, rho: float, shear_as_reference: bool = True) -> np.ndarray:
+    """Material row of the 3D solid (D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55
+    D56 D66 rho, strain order xx yy zz xy yz xz) from a stiffness in the order
+    x y z yz xz xy.  With ``shear_as_reference`` the two transverse shear terms
+    are placed as the reference's composite3D_transf.m:107-108 places them
+    (D55 from the xz term, D66 from the yz term); otherwise D55 = C_yz,yz."""
+    xy, yz, xz = 5, 3, 4
+    D = dict(D11=C[0, 0], D12=C[0, 1], D13=C[0, 2], D14=C[0, xy], D22=C[1, 1], D23=C[1, 2], D24=C[1, xy],
+             D33=C[2, 2], D34=C[2, xy], D44=C[xy, xy])
+    if shear_as_reference:
+        D55, D56, D66 = C[xz, xz], C[yz, xz], C[yz, yz]
+    else:
+        D55, D56, D66 = C[yz, yz], C[yz, xz], C[xz, xz]
+    return np.array([D["D11"], D["D12"], D["D13"], D["D14"], D["D22"], D["D23"], D["D24"], D["D33"], D["D34"],
+                     D["D44"], D55, D56, D66, rho], float)
+
+
+def cfrp_c3d() -> np.ndarray:
+    """3D stiffness of the synthetic CFRP ply (E33 = E22, nu13 = nu12, nu23
+    from G23 = E22 / (2 (1 + nu23)))."""
+    p = CFRP_PLY
+    nu23 = p["E22"] / (2 * p["G23"]) - 1.0
+    return orthotropic_c3d(p["E11"], p["E22"], p["E22"], p["nu12"], p["nu12"], nu23, p["G12"], p["G13"], p["G23"])

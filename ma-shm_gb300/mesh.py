@@ -106,3 +106,74 @@ def circle_sensor_nodes(mesh: dict, xc: float, yc: float, r: float, n: int, phas
     ang = phase + 2 * np.pi * np.arange(n) / n
     return np.array([nearest_node(mesh["coords"], xc + r * np.cos(t), yc + r * np.sin(t)) for t in ang],
                     dtype=np.int32)
+
+
+def solid_plate(Lx: float, Ly: float, nex: int, ney: int, ply_t, order: int = 5, nz: int = 3) -> dict:
+    """Laminate plate of 3D spectral elements, one element per ply through the
+    thickness (order ``order`` in plane, ``nz`` GLL nodes through the ply),
+    as extrude_mesh.m builds it: elements layer by layer (bottom ply first),
+    local nodes x fastest then y then z, global nodes numbered node layer by
+    node layer (in-plane row-major inside a layer).  z runs from -h/2 to +h/2."""
+    base = structured_plate(Lx, Ly, nex, ney, order)
+    ply_t = np.asarray(ply_t, float)
+    nply = len(ply_t)
+    zg, _ = gll_points(nz)
+    NXY = base["coords"].shape[0]
+    h = float(ply_t.sum())
+    zb = -h / 2 + np.concatenate(([0.0], np.cumsum(ply_t)))
+    nlay = (nz - 1) * nply + 1
+    zl = np.empty(nlay)
+    for i in range(nply):
+        for k in range(nz):
+            zl[(nz - 1) * i + k] = zb[i] + (zg[k] + 1) / 2 * ply_t[i]
+    coords = np.zeros((nlay * NXY, 3))
+    coords[:, 0] = np.tile(base["coords"][:, 0], nlay)
+    coords[:, 1] = np.tile(base["coords"][:, 1], nlay)
+    coords[:, 2] = np.repeat(zl, NXY)
+    fen2 = base["nodes"].shape[0]
+    nodes = np.zeros((nply * fen2, base["nodes"].shape[1] * nz), np.int32)
+    npl = base["nodes"].shape[1]
+    for i in range(nply):
+        for k in range(nz):
+            nodes[i * fen2:(i + 1) * fen2, k * npl:(k + 1) * npl] = base["nodes"] + ((nz - 1) * i + k) * NXY
+    return dict(nodes=nodes, coords=coords, nex=nex, ney=ney, nply=nply, nz=nz, NXY=NXY, fen2=fen2,
+                ply_layer_of_element=np.repeat(np.arange(nply), fen2), h=h, base=base)
+
+
+def split_interface(mesh3d: dict, interface: int, elems2d) -> dict:
+    """Delamination between ply layers ``interface`` and ``interface+1``
+    (0-based from the bottom) under the in-plane elements ``elems2d``:
+    interface nodes whose every adjacent in-plane element is delaminated get
+    a copy, and the elements of the upper ply use the copies, so that the two
+    plies are not connected there (the perimeter nodes stay shared).  This is
+    the topology change of split_delam_nodes2.m; no stiffness is added."""
+    nodes = mesh3d["nodes"].copy()
+    coords = mesh3d["coords"]
+    base = mesh3d["base"]
+    nz, fen2, NXY = mesh3d["nz"], mesh3d["fen2"], mesh3d["NXY"]
+    npl = base["nodes"].shape[1]
+    delam = np.zeros(fen2, bool)
+    delam[np.asarray(elems2d, int)] = True
+    # in-plane nodes touched only by delaminated elements
+    touched_bad = np.zeros(NXY + 1, bool)
+    touched_good = np.zeros(NXY + 1, bool)
+    for e in range(fen2):
+        (touched_bad if delam[e] else touched_good)[base["nodes"][e]] = True
+    inner = np.nonzero(touched_bad & ~touched_good)[0]          # 1-based in-plane node ids
+    layer = (nz - 1) * (interface + 1)
+    old = inner + layer * NXY                                   # 1-based global ids
+    new = coords.shape[0] + 1 + np.arange(len(inner))
+    remap = dict(zip(old.tolist(), new.tolist()))
+    upper = slice((interface + 1) * fen2, (interface + 2) * fen2)
+    blk = nodes[upper, :npl]                                    # bottom node layer of the upper ply
+    flat = blk.reshape(-1)
+    for i, g in enumerate(flat):
+        r = remap.get(int(g))
+        if r is not None:
+            flat[i] = r
+    nodes[upper, :npl] = flat.reshape(blk.shape)
+    out = dict(mesh3d)
+    out["nodes"] = nodes
+    out["coords"] = np.concatenate([coords, coords[old - 1]])
+    out["split_nodes"] = old
+    return out

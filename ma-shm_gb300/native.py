@@ -43,6 +43,15 @@ class ShmRun(C.Structure):
                 ("frm_int", C.c_int32), ("frame_dof", C.c_int32)]
 
 
+class ShmSolidMesh(C.Structure):
+    _fields_ = [("fen", C.c_int32), ("npe", C.c_int32), ("nnode", C.c_int32), ("nodes", I32P), ("coords", F64P),
+                ("basket_rows", C.c_int32), ("I_G", I32P), ("I_L", I32P)]
+
+
+class ShmSolidMaterial(C.Structure):
+    _fields_ = [("nmat", C.c_int32), ("table", F64P), ("elem_mat", I32P), ("elem_keep", F64P)]
+
+
 class ShmOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("path", C.c_int32), ("steps_per_graph", C.c_int32),
                 ("tile_elems", C.c_int32), ("device", C.c_int32), ("rows_per_block", C.c_int32)]
@@ -73,6 +82,8 @@ SIGNATURES = {
     "shm_apply_stiffness": (C.c_int, [C.c_void_p, F64P, F64P]),
     "shm_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "shm_mass": (C.c_int, [C.c_void_p, F64P]),
+    "shm_solid_plan_create": (C.c_int, [C.c_int32, C.POINTER(ShmSolidMesh), C.POINTER(ShmSolidMaterial),
+                                        C.POINTER(ShmRun), C.POINTER(ShmOptions), C.POINTER(C.c_void_p)]),
     "shm_forward_backward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_int32, C.c_void_p]),
     "shm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_float)]),

@@ -77,6 +77,7 @@ class Plan:
         self._refresh_info()
         self.nscen = n
         self.nft = run.nft
+        self.nf = 5
 
     def _refresh_info(self):
         info = (C.c_int64 * 9)()
@@ -234,8 +235,8 @@ class Plan:
 
     def get_state(self):
         n = self.info["nnode"]
-        U = np.zeros(5 * n)
-        Uo = np.zeros(5 * n)
+        U = np.zeros(self.nf * n)
+        Uo = np.zeros(self.nf * n)
         self._check(self.lib.shm_get_state(self.handle, native.ptr(U), native.ptr(Uo)))
         return U, Uo
 
@@ -251,9 +252,73 @@ class Plan:
         return F
 
     def mass(self):
-        mg = np.zeros(5 * self.info["nnode"])
+        mg = np.zeros(self.nf * self.info["nnode"])
         self._check(self.lib.shm_mass(self.handle, native.ptr(mg)))
         return mg
+
+
+@dataclass
+class SolidScenario:
+    """One laminate modelled with 3D solid elements (6x6x3 nodes, 3 DOF/node)."""
+    mesh: dict                        # nodes [fen,108] 1-based, coords [nnode,3]
+    mat_table: np.ndarray             # [nmat, 14] (materials.solid_row)
+    elem_mat: np.ndarray | None = None
+    elem_keep: np.ndarray | None = None
+    force_dof: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))   # 3*(node-1)+{1,2,3}
+    force_val: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    out_dof: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    signal: np.ndarray | None = None
+    sensors: list = field(default_factory=list)
+
+
+class SolidPlan(Plan):
+    """3D-solid scenarios on one GPU (shm_solid_plan_create)."""
+
+    def __init__(self, scenarios, run: RunConfig, precision: int = 64, steps_per_graph: int = 0, device: int = 0):
+        self.lib = native.load()
+        self.scenarios = list(scenarios)
+        self.run = run
+        self._keep = []
+        n = len(self.scenarios)
+        meshes = (native.ShmSolidMesh * n)()
+        mats = (native.ShmSolidMaterial * n)()
+        runs = (native.ShmRun * n)()
+        for i, sc in enumerate(self.scenarios):
+            m, mt, r = meshes[i], mats[i], runs[i]
+            nodes = self._arr(np.asarray(sc.mesh["nodes"]).T, np.int32)
+            coords = self._arr(np.asarray(sc.mesh["coords"], float).T, np.float64)
+            m.fen, m.npe = np.asarray(sc.mesh["nodes"]).shape
+            m.nnode = np.asarray(sc.mesh["coords"]).shape[0]
+            m.nodes, m.coords = native.ptr(nodes, native.I32P), native.ptr(coords)
+            m.basket_rows = 0
+            tab = self._arr(np.atleast_2d(sc.mat_table), np.float64)
+            mt.nmat, mt.table = tab.shape[0], native.ptr(tab)
+            mt.elem_mat = native.ptr(self._arr(sc.elem_mat, np.int32), native.I32P) if sc.elem_mat is not None \
+                else None
+            mt.elem_keep = native.ptr(self._arr(sc.elem_keep, np.float64)) if sc.elem_keep is not None else None
+            r.dt, r.nft, r.nn_first = run.dt, run.nft, run.nn_first
+            r.eta_xy, r.eta_z = run.eta_xy, run.eta_z
+            fd, fv = self._arr(sc.force_dof, np.int32), self._arr(sc.force_val, np.float64)
+            r.n_force, r.force_dof, r.force_val = len(fd), native.ptr(fd, native.I32P), native.ptr(fv)
+            od = self._arr(sc.out_dof, np.int32)
+            r.n_out, r.out_dof = len(od), native.ptr(od, native.I32P)
+            r.n_sens = 0
+            r.h = run.h
+            r.frm_int, r.frame_dof = run.frm_int, run.frame_dof
+        opt = native.ShmOptions(precision, 1, steps_per_graph, 0, device, 0)
+        handle = C.c_void_p()
+        st = self.lib.shm_solid_plan_create(n, meshes, mats, runs, C.byref(opt), C.byref(handle))
+        self.handle = handle
+        if st != native.SHM_OK:
+            msg = self.lib.shm_last_error(handle).decode() if handle.value else ""
+            self.lib.shm_plan_destroy(handle)
+            self.handle = None
+            raise native.ShmError(st, msg)
+        self._keep.clear()
+        self._refresh_info()
+        self.nscen = n
+        self.nft = run.nft
+        self.nf = 3
 
 
 # ----------------------------------------------------------------------

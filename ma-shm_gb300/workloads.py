@@ -154,3 +154,53 @@ def plate_pzt(nex=200, L=1.0, T=1e-3, f=100e3, d_pzt=10e-3, t_pzt=0.2e-3, V0=100
     run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"], frm_int=frames_every,
                     frame_dof=5)
     return [sc], run
+
+
+def solid_plate(nex=120, L=0.5, T=0.5e-3, f=50e3, seed=0, n_out=8, radius=0.15, delam=True, nft=None,
+                shear_as_reference=True):
+    """Config 3: CFRP [0/90/45/-45]s plate as 3D solid elements, one element
+    per ply (order 5 in plane, order 2 through the ply), per-ply rotated
+    stiffness, a seeded elliptical delamination (semi-axes U(5, 20) mm) as
+    split interface nodes between two plies, 50 kHz Hann burst as a
+    transverse force at the top-surface centre, ``n_out`` w outputs on the
+    top surface."""
+    from .solver import SolidScenario
+    rng = np.random.default_rng(seed)
+    ply_t = np.array(M.CFRP_PLY_T)
+    angles = np.array(M.CFRP_ANGLES)
+    mesh = MS.solid_plate(L, L, nex, nex, ply_t)
+    C = M.cfrp_c3d()
+    # element layer i is the i-th ply from the bottom; plies are listed from the top
+    rows = np.stack([M.solid_row(M.ply_c3d_rotated(C, angles[len(angles) - 1 - i]), M.CFRP_RHO, shear_as_reference)
+                     for i in range(len(ply_t))])
+    elem_mat = mesh["ply_layer_of_element"].astype(np.int32)
+    info = {}
+    if delam:
+        a, b = rng.uniform(5e-3, 20e-3, 2)
+        xc, yc = rng.uniform(0.25, 0.75, 2) * L
+        interface = int(rng.integers(0, len(ply_t) - 1))
+        els = MS.elements_in_ellipse(mesh["base"], xc, yc, a, b, rng.uniform(0, np.pi))
+        if len(els):
+            mesh = MS.split_interface(mesh, interface, els)
+        info = dict(a=a, b=b, xc=xc, yc=yc, interface=interface, n_split=len(mesh.get("split_nodes", [])))
+    xyz = np.zeros((108, 3))
+    ax = L / nex
+    g6, _ = MS.gll_points(6)
+    g3, _ = MS.gll_points(3)
+    for c in range(108):
+        xyz[c] = ((g6[c % 6] + 1) / 2 * ax, (g6[(c // 6) % 6] + 1) / 2 * ax, (g3[c // 36] + 1) / 2 * ply_t[0])
+    dt = EL.solid_stable_dt(xyz, rows)
+    if nft is None:
+        nft = int(np.ceil(T / dt)) + 1
+    _, st = hanning_signal(dt, nft, f / 5, f, 0.0)
+    NXY = mesh["NXY"]
+    top = (mesh["nz"] - 1) * mesh["nply"] * NXY          # first node of the top node layer (0-based)
+    base = mesh["base"]
+    centre = MS.nearest_node(base["coords"], L / 2, L / 2) + top
+    outs = MS.circle_sensor_nodes(base, L / 2, L / 2, min(radius, 0.45 * L), n_out) + top
+    sc = SolidScenario(mesh=mesh, mat_table=rows, elem_mat=elem_mat,
+                       force_dof=np.array([3 * centre], np.int32), force_val=np.array([1.0]),
+                       out_dof=(3 * outs).astype(np.int32), signal=st)
+    sc.delam = info
+    run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=float(ply_t.sum()))
+    return [sc], run

@@ -204,3 +204,85 @@ class OracleProblem:
                     voltage=voltage[:len(sensors) * nft].reshape(nft, len(sensors)) if sensors else np.zeros((nft, 0)),
                     frames=frames[:nfr * self.nnode].reshape(nfr, self.nnode), U=U, uold=Uo,
                     diverged_at=A.diverged_at, frames_written=A.frames_written)
+
+
+class OracleSolidArgs(C.Structure):
+    _fields_ = [("fen", C.c_int32), ("nnode", C.c_int32), ("nodes", I32P), ("nnz", C.c_int32 * 3),
+                ("row", I32P * 3), ("col", I32P * 3), ("val", F64P * 3), ("invJ", F64P), ("W", F64P),
+                ("D", F64P), ("rows3", C.c_int32), ("IGd", I64P), ("ILd", I64P),
+                ("mg", F64P), ("mg2", F64P), ("mg0", F64P), ("cg", F64P), ("a0", C.c_double), ("a1", C.c_double),
+                ("nn_first", C.c_int32), ("nft", C.c_int32), ("st", F64P), ("Fa", F64P),
+                ("nout", C.c_int32), ("out_dof", I32P), ("displ", F64P), ("nthreads", C.c_int32),
+                ("U", F64P), ("uold", F64P)]
+
+
+class OracleSolid:
+    """Reference-structured set-up of a 3D solid plate (main_spec3Dcuda_global_...)."""
+
+    def __init__(self, nodes1, coords, dtable, rho, elem_mat=None, elem_keep=None):
+        self.nodes = np.ascontiguousarray(nodes1, dtype=np.int32)
+        self.coords = np.asarray(coords, float)
+        fen, npe = self.nodes.shape
+        assert npe == 108
+        self.fen, self.nnode = fen, self.coords.shape[0]
+        Nx, Ny, Nz = R.shape3d_blocks()
+        self.pat = [R.sparse_pattern(N) for N in (Nx, Ny, Nz)]
+        self.invJ, self.W = R.jacobians3d(self.nodes, self.coords, Nx, Ny, Nz)
+        em = np.zeros(fen, np.int64) if elem_mat is None else np.asarray(elem_mat, np.int64)
+        keep = np.ones(fen) if elem_keep is None else np.asarray(elem_keep, float)
+        dt_ = np.atleast_2d(np.asarray(dtable, float))[em] * keep[:, None]          # [fen, 13]
+        self.D = np.ascontiguousarray(np.repeat(dt_.T, 108, axis=1))               # [13, fen*108]
+        rho_e = np.asarray(rho, float)[em] if np.ndim(rho) else np.full(fen, float(rho))
+        I_G, I_L = R.nodes_maps_fiborek(self.nodes, self.nnode, 5, 3)
+        self.Gd, self.Ld = R.basket_dofs(I_G, I_L, 3)
+        self.ndof = 3 * self.nnode
+        mgL = np.repeat(self.W * np.repeat(rho_e, 108), 3)                           # mass3D_v2.m
+        self.mg_raw = R.basket_scatter(mgL, self.Gd, self.Ld, self.ndof)
+
+    def run(self, dt, nft, st, nn_first=2, eta_xy=0.0, eta_z=0.0, force_dof=(), force_val=(), out_dof=(),
+            nthreads=0):
+        a0, a1 = 1 / dt ** 2, 1 / (2 * dt)
+        dv = np.zeros(self.ndof)
+        dv[0::3] = eta_xy
+        dv[1::3] = eta_xy
+        dv[2::3] = eta_z
+        mg = self.mg_raw
+        cg = dv * mg
+        mg2 = 2 * a0 * mg
+        mgs = a0 * mg
+        mg0 = 1.0 / (mgs + a1 * cg)
+        A = OracleSolidArgs()
+        keep = [mg2, mgs, mg0, cg]
+        A.fen, A.nnode = self.fen, self.nnode
+        A.nodes = _p(self.nodes, I32P)
+        for k in range(3):
+            r, c_, v = self.pat[k]
+            A.nnz[k] = len(r)
+            A.row[k], A.col[k], A.val[k] = _p(r, I32P), _p(c_, I32P), _p(v)
+        A.invJ, A.W, A.D = _p(self.invJ), _p(self.W), _p(self.D)
+        Gd = np.ascontiguousarray(self.Gd.T)
+        Ld = np.ascontiguousarray(self.Ld.T)
+        keep += [Gd, Ld]
+        A.rows3 = self.Gd.shape[0]
+        A.IGd, A.ILd = _p(Gd, I64P), _p(Ld, I64P)
+        A.mg, A.mg2, A.mg0, A.cg = _p(mgs), _p(mg2), _p(mg0), _p(cg)
+        A.a0, A.a1 = a0, a1
+        A.nn_first, A.nft = nn_first, nft
+        st = np.ascontiguousarray(st, float)
+        A.st = _p(st)
+        Fa = np.zeros(self.ndof)
+        for d, v in zip(force_dof, force_val):
+            Fa[int(d) - 1] += v
+        A.Fa = _p(Fa)
+        od = np.ascontiguousarray(out_dof, np.int32)
+        displ = np.zeros(max(len(od), 1) * nft)
+        A.nout, A.out_dof, A.displ = len(od), _p(od, I32P), _p(displ)
+        A.nthreads = nthreads
+        U = np.zeros(self.ndof)
+        Uo = np.zeros(self.ndof)
+        A.U, A.uold = _p(U), _p(Uo)
+        lib = _load()
+        lib.oracle_solid_run.restype = C.c_int
+        lib.oracle_solid_run.argtypes = [C.POINTER(OracleSolidArgs)]
+        assert lib.oracle_solid_run(C.byref(A)) == 0
+        return dict(displ=displ[:len(od) * nft].reshape(nft, len(od)), U=U, uold=Uo, mass=self.mg_raw)

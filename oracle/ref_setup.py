@@ -568,3 +568,76 @@ def pzt_actuator_forces(nodes1, coords, pztEl0, pzt_t, h, V0, epzt, gpzt, nx=6, 
     Fa[1::5] = FaxG * (h / 2 + pzt_t / 2)
     Fa[3::5] = FayG * (h / 2 + pzt_t / 2)
     return Fa
+
+
+# --------------------------------------------------------------------------
+# 3D solid set-up (src/models/solid3D)
+# --------------------------------------------------------------------------
+
+
+def shape3d_blocks(nx=6, ny=6, nz=3):
+    """Element blocks of Npx, Npy, Npz (main_spec3Dcuda_global_...:440-470 via
+    shape3D_prim_v2.m evaluated at the GLL nodes, row = node c, x fastest)."""
+    ksi, _ = gll(nx)
+    eta, _ = gll(ny)
+    dz, _ = gll(nz)
+    Qx, Qy, Qz = vandermonde(ksi), vandermonde(eta), vandermonde(dz)
+    n = nx * ny * nz
+    Nx, Ny, Nz = np.zeros((n, n)), np.zeros((n, n)), np.zeros((n, n))
+    c = 0
+    for kz in range(nz):
+        for ky in range(ny):
+            for kx in range(nx):
+                Nx[c], Ny[c], Nz[c] = shape3d_prim(nx, ny, nz, Qx, Qy, Qz, ksi[kx], eta[ky], dz[kz])
+                c += 1
+    return Nx, Ny, Nz
+
+
+def jacobians3d(nodes1, coords, Nx, Ny, Nz, nx=6, ny=6, nz=3):
+    """J11 = Npx*X ... J33 = Npz*Z (:480-488); invJ = J^-1 of
+    [[J11 J12 J13];[J21 J22 J23];[J31 J32 J33]] (inv_jacp.m is not in the
+    reference tree; its use in strains_spec_p.m fixes it as the inverse);
+    WWWDetJ = w_x w_y w_z det J (:600-619)."""
+    X = coords[nodes1 - 1, 0]
+    Y = coords[nodes1 - 1, 1]
+    Z = coords[nodes1 - 1, 2]
+    fen = nodes1.shape[0]
+    J = np.zeros((fen, Nx.shape[0], 3, 3))
+    for a, Np in enumerate((Nx, Ny, Nz)):
+        J[:, :, 0, a] = X @ Np.T
+        J[:, :, 1, a] = Y @ Np.T
+        J[:, :, 2, a] = Z @ Np.T
+    inv = np.linalg.inv(J)
+    det = np.linalg.det(J)
+    _, wx = gll(nx)
+    _, wy = gll(ny)
+    _, wz = gll(nz)
+    www = np.einsum("k,j,i->kji", wz, wy, wx).reshape(-1)
+    invJ = np.stack([inv[:, :, a, b].reshape(-1) for a in range(3) for b in range(3)])  # invJ_ab
+    return invJ, (np.tile(www, fen) * det.reshape(-1))
+
+
+def composite3d_ply(q11, q12, q13, q22, q23, q33, q44, q55, q66, alpha_deg):
+    """Rotated ply constants, composite3D_transf_C.m:18-37, arranged as
+    composite3D_transf.m:113-118 arranges them into D (D55 = s55, D56 = s45,
+    D66 = s44).  Returns the 13 D entries of stresses_spec_p.m."""
+    ar = alpha_deg * np.pi / 180
+    m, n = np.cos(ar), np.sin(ar)
+    if abs(m) < np.finfo(float).eps:
+        m = 0.0
+    if abs(n) < np.finfo(float).eps:
+        n = 0.0
+    s11 = q11 * m ** 4 + 2 * (q12 + 2 * q66) * m ** 2 * n ** 2 + q22 * n ** 4
+    s12 = (q11 + q22 - 4 * q66) * m ** 2 * n ** 2 + q12 * (m ** 4 + n ** 4)
+    s13 = q13 * m ** 2 + q23 * n ** 2
+    s16 = (q11 - q12 - 2 * q66) * m ** 3 * n + (q12 - q22 + 2 * q66) * m * n ** 3
+    s22 = q11 * n ** 4 + 2 * (q12 + 2 * q66) * m ** 2 * n ** 2 + q22 * m ** 4
+    s23 = n ** 2 * q13 + m ** 2 * q23
+    s33 = q33
+    s26 = (q11 - q12 - 2 * q66) * n ** 3 * m + (q12 - q22 + 2 * q66) * n * m ** 3
+    s36 = (q13 - q23) * m * n
+    s44 = q44 * m ** 2 + q55 * n ** 2
+    s45 = (q55 - q44) * m * n
+    s55 = q55 * m ** 2 + q44 * n ** 2
+    s66 = (q11 + q22 - 2 * q12 - 2 * q66) * m ** 2 * n ** 2 + q66 * (m ** 4 + n ** 4)
+    return np.array([s11, s12, s13, s16, s22, s23, s26, s33, s36, s66, s55, s45, s44])

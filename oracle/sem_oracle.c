@@ -305,3 +305,149 @@ int oracle_flat_shell_apply_k(oracle_args *A, double *Fout) {
   free(zero); free(minus1); free(U); free(uo);
   return rc;
 }
+
+/* ------------------------------------------------------------------------
+ * 3D solid loop: src/models/solid3D/main_spec3Dcuda_global_cpu_gpu3_wave_sens_opt_single_PCT_mat.m:922-1040
+ * strains_spec_p.m, stresses_spec_p.m, forces :944-954, 12-basket scatter,
+ * update :1032-1037, outputs U(outputs).  Element blocks of Npx, Npy, Npz
+ * (108 x 108) as nonzero lists in MATLAB find() order.
+ * ------------------------------------------------------------------------ */
+#define SNPE 108
+
+typedef struct {
+  int32_t fen, nnode;
+  const int32_t *nodes; /* [fen*108] element-major, 1-based */
+  int32_t nnz[3];
+  const int32_t *row[3], *col[3];
+  const double *val[3];
+  const double *invJ;   /* [9][fen*108]: invJ11 invJ12 invJ13 invJ21 ... invJ33 */
+  const double *W;      /* [fen*108] WWWDetJ */
+  const double *D;      /* [13][fen*108]: D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55 D56 D66 */
+  int32_t rows3;
+  const int64_t *IGd, *ILd; /* [rows3*12] column-major, 1-based, 3-dof numbering */
+  const double *mg, *mg2, *mg0, *cg;
+  double a0, a1;
+  int32_t nn_first, nft;
+  const double *st;
+  const double *Fa;
+  int32_t nout;
+  const int32_t *out_dof;
+  double *displ;
+  int32_t nthreads;
+  double *U, *uold;
+} oracle_solid_args;
+
+static inline void sp3(int nnz, const int32_t *row, const int32_t *col, const double *val, const double *x, double *y) {
+  for (int c = 0; c < SNPE; ++c) y[c] = 0.0;
+  for (int k = 0; k < nnz; ++k) y[row[k]] += val[k] * x[col[k]];
+}
+static inline void sp3t(int nnz, const int32_t *row, const int32_t *col, const double *val, const double *x, double *y) {
+  for (int c = 0; c < SNPE; ++c) y[c] = 0.0;
+  for (int k = 0; k < nnz; ++k) y[col[k]] += val[k] * x[row[k]];
+}
+
+int oracle_solid_run(oracle_solid_args *A) {
+  const int fen = A->fen;
+  const int L = fen * SNPE;
+  const int ndof = 3 * A->nnode;
+#ifdef _OPENMP
+  if (A->nthreads > 0) omp_set_num_threads(A->nthreads);
+#endif
+  double *F2 = (double *)calloc((size_t)3 * L, sizeof(double));
+  double *F = (double *)calloc((size_t)ndof, sizeof(double));
+  double *unew = (double *)calloc((size_t)ndof, sizeof(double));
+  if (!F2 || !F || !unew) return -1;
+  double *U = A->U, *uold = A->uold;
+  for (int nn = A->nn_first; nn <= A->nft; ++nn) {
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < fen; ++e) {
+      double UX[SNPE], UY[SNPE], UZ[SNPE], d[9][SNPE];
+      const int32_t *nd = A->nodes + (size_t)e * SNPE;
+      for (int c = 0; c < SNPE; ++c) {
+        UX[c] = U[3 * nd[c] - 3];
+        UY[c] = U[3 * nd[c] - 2];
+        UZ[c] = U[3 * nd[c] - 1];
+      }
+      /* d[3*k + f]: Np{x,y,z}[k] * U{X,Y,Z}[f] */
+      const double *Uf[3] = {UX, UY, UZ};
+      for (int k = 0; k < 3; ++k)
+        for (int f = 0; f < 3; ++f) sp3(A->nnz[k], A->row[k], A->col[k], A->val[k], Uf[f], d[3 * k + f]);
+      const size_t l0 = (size_t)e * SNPE;
+#define IJ(a, b) A->invJ[(size_t)(3 * (a) + (b)) * L + l0 + c]
+#define DD(k) A->D[(size_t)(k) * L + l0 + c]
+      double Sxx[SNPE], Syy[SNPE], Szz[SNPE], Sxy[SNPE], Syz[SNPE], Sxz[SNPE];
+      for (int c = 0; c < SNPE; ++c) {
+        /* strains_spec_p.m:8-27 (NpxU = d[0..2], NpyU = d[3..5], NpzU = d[6..8]) */
+        const double Exx = (d[0][c]) * IJ(0, 0) + (d[3][c]) * IJ(1, 0) + (d[6][c]) * IJ(2, 0);
+        const double Eyy = (d[1][c]) * IJ(0, 1) + (d[4][c]) * IJ(1, 1) + (d[7][c]) * IJ(2, 1);
+        const double Ezz = (d[2][c]) * IJ(0, 2) + (d[5][c]) * IJ(1, 2) + (d[8][c]) * IJ(2, 2);
+        const double B41UX = (d[0][c]) * IJ(0, 1) + (d[3][c]) * IJ(1, 1) + (d[6][c]) * IJ(2, 1);
+        const double B42UY = (d[1][c]) * IJ(0, 0) + (d[4][c]) * IJ(1, 0) + (d[7][c]) * IJ(2, 0);
+        const double Exy = B41UX + B42UY;
+        const double B52UY = (d[1][c]) * IJ(0, 2) + (d[4][c]) * IJ(1, 2) + (d[7][c]) * IJ(2, 2);
+        const double B53UZ = (d[2][c]) * IJ(0, 1) + (d[5][c]) * IJ(1, 1) + (d[8][c]) * IJ(2, 1);
+        const double Eyz = B52UY + B53UZ;
+        const double B61UX = (d[0][c]) * IJ(0, 2) + (d[3][c]) * IJ(1, 2) + (d[6][c]) * IJ(2, 2);
+        const double B63UZ = (d[2][c]) * IJ(0, 0) + (d[5][c]) * IJ(1, 0) + (d[8][c]) * IJ(2, 0);
+        const double Exz = B61UX + B63UZ;
+        /* stresses_spec_p.m:5-10 */
+        Sxx[c] = Exx * DD(0) + Eyy * DD(1) + Ezz * DD(2) + Exy * DD(3);
+        Syy[c] = Exx * DD(1) + Eyy * DD(4) + Ezz * DD(5) + Exy * DD(6);
+        Szz[c] = Exx * DD(2) + Eyy * DD(5) + Ezz * DD(7) + Exy * DD(8);
+        Sxy[c] = Exx * DD(3) + Eyy * DD(6) + Ezz * DD(8) + Exy * DD(9);
+        Syz[c] = Eyz * DD(10) + Exz * DD(11);
+        Sxz[c] = Eyz * DD(11) + Exz * DD(12);
+      }
+      /* forces, :944-954: f = sum over terms left to right */
+      const double *W = A->W + l0;
+      double acc[SNPE], tmp[SNPE], v_[SNPE];
+#define T3(first, S, a, b, k)                                                     \
+  do {                                                                            \
+    for (int c = 0; c < SNPE; ++c) v_[c] = S[c] * IJ(a, b) * W[c];                \
+    sp3t(A->nnz[k], A->row[k], A->col[k], A->val[k], v_, tmp);                    \
+    if (first) for (int c = 0; c < SNPE; ++c) acc[c] = tmp[c];                    \
+    else for (int c = 0; c < SNPE; ++c) acc[c] = acc[c] + tmp[c];                 \
+  } while (0)
+      double *f2 = F2 + 3 * l0;
+      /* fu: Sxx (invJ11,21,31), Sxy (invJ12,22,32), Sxz (invJ13,23,33) */
+      T3(1, Sxx, 0, 0, 0); T3(0, Sxx, 1, 0, 1); T3(0, Sxx, 2, 0, 2);
+      T3(0, Sxy, 0, 1, 0); T3(0, Sxy, 1, 1, 1); T3(0, Sxy, 2, 1, 2);
+      T3(0, Sxz, 0, 2, 0); T3(0, Sxz, 1, 2, 1); T3(0, Sxz, 2, 2, 2);
+      for (int c = 0; c < SNPE; ++c) f2[3 * c + 0] = acc[c];
+      /* fv: Syy (12,22,32), Sxy (11,21,31), Syz (13,23,33) */
+      T3(1, Syy, 0, 1, 0); T3(0, Syy, 1, 1, 1); T3(0, Syy, 2, 1, 2);
+      T3(0, Sxy, 0, 0, 0); T3(0, Sxy, 1, 0, 1); T3(0, Sxy, 2, 0, 2);
+      T3(0, Syz, 0, 2, 0); T3(0, Syz, 1, 2, 1); T3(0, Syz, 2, 2, 2);
+      for (int c = 0; c < SNPE; ++c) f2[3 * c + 1] = acc[c];
+      /* fw: Szz (13,23,33), Syz (12,22,32), Sxz (11,21,31) */
+      T3(1, Szz, 0, 2, 0); T3(0, Szz, 1, 2, 1); T3(0, Szz, 2, 2, 2);
+      T3(0, Syz, 0, 1, 0); T3(0, Syz, 1, 1, 1); T3(0, Syz, 2, 1, 2);
+      T3(0, Sxz, 0, 0, 0); T3(0, Sxz, 1, 0, 1); T3(0, Sxz, 2, 0, 2);
+      for (int c = 0; c < SNPE; ++c) f2[3 * c + 2] = acc[c];
+#undef T3
+#undef IJ
+#undef DD
+    }
+    memset(F, 0, sizeof(double) * ndof);
+    for (int b = 0; b < 12; ++b) {
+      const int64_t *g = A->IGd + (size_t)b * A->rows3;
+      const int64_t *l = A->ILd + (size_t)b * A->rows3;
+#pragma omp parallel for schedule(static)
+      for (int r = 0; r < A->rows3; ++r)
+        if (g[r] > 0) F[g[r] - 1] = F[g[r] - 1] + F2[l[r] - 1];
+    }
+    const double s_nn = A->st[nn - 1];
+#pragma omp parallel for schedule(static)
+    for (int dd = 0; dd < ndof; ++dd) {
+      double f = -F[dd] + A->mg2[dd] * U[dd] + A->Fa[dd] * s_nn - A->mg[dd] * uold[dd] + A->a1 * A->cg[dd] * uold[dd];
+      unew[dd] = A->mg0[dd] * f;
+    }
+    for (int k = 0; k < A->nout; ++k) A->displ[(size_t)(nn - 1) * A->nout + k] = U[A->out_dof[k] - 1];
+    memcpy(uold, U, sizeof(double) * ndof);
+    memcpy(U, unew, sizeof(double) * ndof);
+  }
+  free(F2);
+  free(F);
+  free(unew);
+  return 0;
+}

@@ -163,3 +163,27 @@ def test_pzt_actuator_loads_match_reference(pkg, nex, elems):
     assert np.linalg.norm(Fp - Fo) <= 1e-12 * np.linalg.norm(Fo)
     assert abs(Fp[0::5].sum()) <= 1e-12 * np.abs(Fp[0::5]).max()
     assert abs(Fp[2::5].sum()) <= 1e-12 * np.abs(Fp[2::5]).max()
+
+
+@pytest.mark.parametrize("angle", [0.0, 90.0, 45.0, -45.0, 30.0])
+def test_solid_ply_stiffness_matches_reference(pkg, angle):
+    """Bond-matrix rotation + D arrangement == composite3D_transf_C.m:18-37 with
+    composite3D_transf.m:113-118 (D55 = s55, D56 = s45, D66 = s44)."""
+    M = pkg.materials
+    C = M.cfrp_c3d()
+    row = M.solid_row(M.ply_c3d_rotated(C, angle), 1570.0)[:13]
+    ref = R.composite3d_ply(C[0, 0], C[0, 1], C[0, 2], C[1, 1], C[1, 2], C[2, 2], C[3, 3], C[4, 4], C[5, 5], angle)
+    assert np.abs(row - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_solid_mesh_and_delamination_split(pkg):
+    m = pkg.mesh.solid_plate(0.02, 0.02, 4, 4, [0.5e-3] * 3)
+    assert m["nodes"].shape == (48, 108)
+    assert m["nodes"].max() == m["coords"].shape[0]
+    d = pkg.mesh.split_interface(m, 0, [5, 6, 9, 10])
+    # the 2x2 patch has 3x3 interior corner+edge lines of nodes: (2*5-1)^2 inner nodes
+    assert len(d["split_nodes"]) == 81
+    upper = d["nodes"][16:32, :36]
+    lower = d["nodes"][0:16, 72:]
+    assert len(np.intersect1d(upper, lower)) == len(np.unique(lower)) - 81
+    np.testing.assert_allclose(d["coords"][-81:], m["coords"][d["split_nodes"] - 1])
