@@ -214,6 +214,28 @@ def adjoint_bench(pkg, args):
     print(json.dumps(out))
 
 
+def plain_fp64_bench(pkg, args):
+    """Reference-structured FP64 GPU loop on single scenarios: one plate of
+    the batch workload and the 200x200-element plate; outputs checked against
+    the engine's FP64 path over the same steps."""
+    from baseline.plain_gpu_fp64 import rate
+    W = pkg.workloads
+    out = {"metric": "plain single-scenario FP64 GPU path, DOF-steps/s"}
+    cases = {"batch_plate": W.batch(n=1, seed=0), "plate_200x200_pzt": W.plate_pzt()}
+    for name, (scs, run) in cases.items():
+        steps = 40
+        v, displ = rate(pkg, scs[0], run, steps=steps, warmup=5)
+        p = pkg.Plan(scs, run, precision=64, path=1)
+        p.reset()
+        p.set_signal()
+        p.advance(steps + 5)
+        ref = p.read_outputs()[0]["displ"][run.nn_first - 1: run.nn_first - 1 + steps + 5]
+        p.close()
+        err = float(np.linalg.norm(displ - ref) / max(np.linalg.norm(ref), 1e-300)) if np.abs(ref).max() > 0 else 0.0
+        out[name] = {"dof": W.dof_count(scs), "dof_steps_per_s": v, "rel_err_vs_engine_fp64": err, "steps": steps}
+    print(json.dumps(out))
+
+
 def single_plate_bench(pkg, args):
     """One plate (config 1 or 2): whole forward solve in FP64 and FP32 through
     shm_forward (outputs, PZT voltage, frames), FP32 error vs the FP64 run."""
@@ -279,6 +301,8 @@ def main():
                     help="batch: 512 plates (default); force: 20x20-element plate; pzt: 200x200 plate with PZT")
     ap.add_argument("--adj-maps", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=20000)
+    ap.add_argument("--plain-fp64", action="store_true",
+                    help="time the reference-structured FP64 GPU loop (the 30x denominator)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -287,6 +311,8 @@ def main():
     pkg = g.package()
     if args.adjoint:
         return adjoint_bench(pkg, args)
+    if args.plain_fp64:
+        return plain_fp64_bench(pkg, args)
     if args.workload != "batch":
         return single_plate_bench(pkg, args)
     W = pkg.workloads
