@@ -95,23 +95,34 @@ class ClockSampler:
 
 
 def dist_init(args):
+    """Rank, world size and local rank from torchrun's environment.  The GPU arm
+    uses NCCL (barrier and max of the timers only: plates are independent, so
+    the data path has no collective); the CPU reference arm uses gloo."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
         import torch
         import torch.distributed as dist
         rank = int(os.environ["RANK"])
         local = int(os.environ.get("LOCAL_RANK", rank))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return rank, ws, local
     return 0, 1, 0
+
+
+def _on_gpu():
+    import torch.distributed as dist
+    return dist.get_backend() == "nccl"
 
 
 def barrier_sync(ws):
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.synchronize()
+        if _on_gpu():
+            torch.cuda.synchronize()
         dist.barrier()
 
 
@@ -120,9 +131,15 @@ def max_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _on_gpu() else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_batch(W, plates, rank):
+    """This rank's shard: its own `plates` plates, seeded by the rank (weak
+    scaling: per-rank work is fixed as the number of ranks grows)."""
+    return W.batch(n=plates, seed=1000 * rank)
 
 
 def cpu_reference(scenarios, run, steps, nthreads=0, budget_s=20.0):
@@ -316,7 +333,7 @@ def main():
     if args.workload != "batch":
         return single_plate_bench(pkg, args)
     W = pkg.workloads
-    scs, run = W.batch(n=args.plates, seed=1000 * rank)
+    scs, run = rank_batch(W, args.plates, rank)
     ndof = W.dof_count(scs)
     config = {"workload": f"batch of {args.plates} flat-shell plates, U{{40..80}}^2 order-5 elements (6.25 mm), "
                           f"1-3 damage zones, random actuator, 5-cycle Hann {{50,75,100}} kHz, 0.4 ms",

@@ -109,7 +109,7 @@ const char *shm_last_error(const shm_plan *plan);
 
 /* Whole forward solve, the MAIN LOOP (main_flat_shell.m:651-917).
  *   st      [nscen][nft]            excitation samples st(nn) (Hanning_signal.m)
- *   displ   [nscen][n_out x nft]    column-major per scenario (displ, :926)
+ *   displ   [nscen][nft x n_out]    column-major per scenario (displ, :926)
  *   voltage [nscen][nft x n_sens]   column-major per scenario (voltage, :925)
  *   frames  [nscen][nframes x nnode] velocity frames, frame-major (V?_frame<c>)
  * Any output pointer may be NULL.  `stream` is a cudaStream_t or NULL. */

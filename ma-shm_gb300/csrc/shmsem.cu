@@ -1335,16 +1335,6 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
   return shm_reset(p);
 }
 
-// helper used by the structured builder to register device allocations
-extern "C" void* shm__plan_alloc(void* plan, size_t bytes) {
-  shm_plan* p = (shm_plan*)plan;
-  void* q = nullptr;
-  if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
-  cudaMemset(q, 0, std::max<size_t>(bytes, 16));
-  p->allocs.push_back(q);
-  return q;
-}
-
 extern "C" shm_status shm_plan_destroy(shm_plan* p) {
   if (!p) return SHM_OK;
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
