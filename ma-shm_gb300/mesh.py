@@ -177,3 +177,72 @@ def split_interface(mesh3d: dict, interface: int, elems2d) -> dict:
     out["coords"] = np.concatenate([coords, coords[old - 1]])
     out["split_nodes"] = old
     return out
+
+
+def boundary_nodes(mesh: dict) -> np.ndarray:
+    """1-based ids of every node on the outer boundary of a structured plate,
+    GLL edge nodes included (the ``boundary_nodes`` output of
+    quad2spectral_Fiborek.m:156)."""
+    NX, NY = mesh["NX"], mesh["NY"]
+    g = np.arange(NX * NY).reshape(NY, NX)
+    return np.unique(np.concatenate([g[0], g[-1], g[:, 0], g[:, -1]])) + 1
+
+
+def split_delam_nodes_flat_shell(nodes: np.ndarray, coords: np.ndarray, den, boundary, order: int = 5):
+    """Delamination topology of the flat shell (split_delam_nodes_flat_shell.m:37-268).
+
+    The delaminated elements ``den`` (0-based) are duplicated: the originals
+    become the sub-laminate under the delamination (``den_under``) and the
+    copies, appended as elements fen, fen+1, ..., the one above it
+    (``den_above``).  Nodes of the delaminated region are split (the copies
+    get new ids with the same coordinates) except the region's outer nodes,
+    which both sub-laminates and the intact plate keep sharing:
+
+    * a corner node is outer when at most two delaminated elements have it as
+      a corner (a corner shared by three, the inside of an L, counts as inner,
+      as in the reference);
+    * an edge node is outer when no other delaminated element has it on an edge;
+    * outer nodes on the plate's boundary are split anyway, except the
+      "free" corners (corner of a single delaminated element) lying on the
+      boundary; with three of those the smallest id is split too.
+
+    Counts are the reference's pairwise neighbour loops rewritten as
+    occurrence counts (an element's own corner/edge positions hold a node at
+    most once).  Inner nodes get new ids in ascending order of the old ids.
+    Returns (nodes, coords, den_under, den_above) with 1-based node ids.
+    """
+    nodes = np.asarray(nodes)
+    coords = np.asarray(coords, dtype=float)
+    den = np.asarray(den, dtype=np.int64).reshape(-1)
+    fen, npe = nodes.shape
+    n = order + 1
+    if npe != n * n:
+        raise ValueError("nodes must have (order+1)^2 columns")
+    loc = np.arange(npe).reshape(n, n)                              # [eta, xi]
+    corner_pos = np.array([loc[0, 0], loc[0, -1], loc[-1, 0], loc[-1, -1]])
+    edge_pos = np.concatenate([loc[0, 1:-1], loc[1:-1, -1], loc[-1, 1:-1], loc[1:-1, 0]])
+    nm = int(nodes.max())
+    sub = nodes[den]                                                # [nd, npe]
+    cn = sub[:, corner_pos].reshape(-1)
+    en = sub[:, edge_pos].reshape(-1)
+    ccount = np.bincount(cn, minlength=nm + 1)
+    ecount = np.bincount(en, minlength=nm + 1)
+    outer = np.concatenate([cn[ccount[cn] <= 2], en[ecount[en] == 1]])
+    free_corner = cn[ccount[cn] == 1]
+    special = np.intersect1d(free_corner, np.asarray(boundary))
+    if special.size == 3:
+        special = special[1:]
+    outer = np.union1d(np.setdiff1d(np.unique(outer), np.asarray(boundary)), special)
+    inner = np.setdiff1d(np.unique(sub), outer)
+    new_id = np.zeros(nm + 1, dtype=np.int64)
+    new_id[inner] = nm + 1 + np.arange(inner.size)
+    above = sub.copy()
+    hit = new_id[above] > 0
+    above[hit] = new_id[above[hit]]
+    out_nodes = np.concatenate([nodes, above.astype(nodes.dtype)])
+    nmax = nm + inner.size
+    out_coords = np.zeros((nmax, coords.shape[1]))
+    out_coords[:min(nm, coords.shape[0])] = coords[:nm]
+    out_coords[above - 1] = out_coords[sub - 1]
+    den_above = fen + np.arange(den.size)
+    return out_nodes, out_coords, den.copy(), den_above

@@ -53,6 +53,42 @@ def plate_force(nex=20, ney=20, L=0.5, T=0.5e-3, f=50e3, n_out=8, radius=0.15, d
     return [sc], run
 
 
+def plate_delamination(nex=20, ney=20, L=0.5, T=0.5e-3, f=50e3, zone=(0.32, 0.30, 0.06, 0.035, 0.5),
+                       layer=4, n_out=8, radius=0.15, nft=None):
+    """Plate of ``plate_force`` with one delamination between plies ``layer``
+    and ``layer + 1`` (counted from the top surface) under an elliptical zone
+    (xc, yc, a, b, angle in m / rad): the zone's elements are split into the
+    sub-laminate above (plies 0..layer-1) and under (plies layer..) the
+    delamination (split_delam_nodes_flat_shell.m, composite_plate_c_delam.m:88-173),
+    both integrated about the intact laminate's mid-plane."""
+    lam = M.cfrp_laminate()
+    q = M.ply_stiffness(**M.CFRP_PLY)
+    nply = len(M.CFRP_PLY_T)
+    above = M.laminate(q, M.CFRP_RHO, M.CFRP_PLY_T, M.CFRP_ANGLES, plies=range(layer))
+    under = M.laminate(q, M.CFRP_RHO, M.CFRP_PLY_T, M.CFRP_ANGLES, plies=range(layer, nply))
+    base = MS.structured_plate(L, L, nex, ney)
+    den = MS.elements_in_ellipse(base, *zone)
+    nodes, coords, den_under, den_above = MS.split_delam_nodes_flat_shell(base["nodes"], base["coords"], den,
+                                                                          MS.boundary_nodes(base))
+    mesh = dict(nodes=nodes, coords=coords, structured=False, mesh_min=base["mesh_min"],
+                mesh_max=base["mesh_max"], den_under=den_under, den_above=den_above, base=base)
+    elem_mat = np.zeros(nodes.shape[0], np.int32)
+    elem_mat[den_under] = 2
+    elem_mat[den_above] = 1
+    table = np.stack([M.table_row(lam), M.table_row(above), M.table_row(under)])
+    dt = _dt_for(L / nex, L / ney, [lam, above, under])
+    if nft is None:
+        nft = int(np.ceil(T / dt)) + 1
+    centre = MS.nearest_node(base["coords"], L / 2, L / 2)
+    outs = MS.circle_sensor_nodes(base, L / 2, L / 2, min(radius, 0.45 * L), n_out)
+    _, st = hanning_signal(dt, nft, f / 5, f, 0.0)
+    sc = Scenario(mesh=mesh, mat_table=table, elem_mat=elem_mat,
+                  force_dof=np.array([5 * centre], np.int32), force_val=np.array([1.0]),
+                  out_dof=(5 * outs).astype(np.int32), signal=st)
+    run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return [sc], run
+
+
 def random_plate(rng, edge=6.25e-3, nmin=40, nmax=80, lam=None, n_out=8, freqs=(50e3, 75e3, 100e3),
                  dt=None, nft=None):
     """One scenario of the batched workload (damage zones, actuator, carrier)."""

@@ -641,3 +641,78 @@ def composite3d_ply(q11, q12, q13, q22, q23, q33, q44, q55, q66, alpha_deg):
     s55 = q55 * m ** 2 + q44 * n ** 2
     s66 = (q11 + q22 - 2 * q12 - 2 * q66) * m ** 2 * n ** 2 + q66 * (m ** 4 + n ** 4)
     return np.array([s11, s12, s13, s16, s22, s23, s26, s33, s36, s66, s55, s45, s44])
+
+
+# --------------------------------------------------------------------------
+# delamination topology
+# --------------------------------------------------------------------------
+
+
+def split_delam_nodes_flat_shell(nodes, coords, den1, nx, ny, boundary_nodes):
+    """``src/models/flat_shell/mesher/split_delam_nodes_flat_shell.m:37-268``,
+    literally: the per-element neighbour loops over corners and the four edge
+    lists, the free-corner / boundary rule, then the split in ascending order
+    of the inner node ids.  ``den1`` holds 1-based element numbers as in the
+    reference; returns (nodes, coords, den_under, den_above), 1-based."""
+    nodes = np.array(nodes, dtype=np.int64)
+    coords = np.asarray(coords, dtype=float)
+    den = [int(e) for e in den1]
+    fen = nodes.shape[0]
+    mc = [1, nx, nx * ny - nx + 1, nx * ny]
+    edge1 = list(range(2, nx))
+    edge2 = [(k + 1) * nx for k in range(1, ny - 1)]
+    edge3 = list(range(nx * ny - nx + 2, nx * ny))
+    edge4 = [k * nx + 1 for k in range(1, ny - 1)]
+    den_under = list(den)
+    den_above = [fen + k for k in range(1, len(den) + 1)]
+    delamnodes = sorted(set(nodes[[e - 1 for e in den]].reshape(-1).tolist())) if den else []
+    nodemax = int(nodes.max())
+    nm = nodemax
+    nodes = np.concatenate([nodes, nodes[[e - 1 for e in den]]]) if den else nodes
+
+    def at(elem1, pos1):
+        return int(nodes[elem1 - 1, pos1 - 1])
+
+    outernodes, free_corner = [], []
+    for k in range(len(den)):
+        others = [j for j in range(len(den)) if j != k]
+        for i in range(4):
+            cn = at(den_above[k], mc[i])
+            neighbours = 0
+            for j in others:
+                for jc in range(4):
+                    if at(den_above[j], mc[jc]) == cn:
+                        neighbours += 1
+            if neighbours in (0, 1):
+                outernodes.append(cn)
+            if neighbours == 0:
+                free_corner.append(cn)
+        for edge in (edge1, edge2, edge3, edge4):
+            for pos in edge:
+                en = at(den_above[k], pos)
+                neighbours = 0
+                for j in others:
+                    for lst in (edge1, edge2, edge3, edge4):
+                        for jc in lst:
+                            if at(den_above[j], jc) == en:
+                                neighbours += 1
+                if neighbours == 0:
+                    outernodes.append(en)
+    bset = set(int(b) for b in np.asarray(boundary_nodes).reshape(-1))
+    special_corner = sorted(set(free_corner) & bset)
+    if len(special_corner) == 3:
+        special_corner = special_corner[1:3]
+    outer = sorted(set(outernodes) - bset) + special_corner
+    innernodes = sorted(set(delamnodes) - set(outer))
+    for node in innernodes:
+        nodemax += 1
+        for i in range(len(den)):
+            for j in range(nx * ny):
+                if nodes[den_above[i] - 1, j] == node:
+                    nodes[den_above[i] - 1, j] = nodemax
+    coords_new = np.zeros((nodemax, 3))
+    coords_new[:nm, :] = coords[:nm, :3]
+    for a, u in zip(den_above, den_under):
+        for j in range(nx * ny):
+            coords_new[nodes[a - 1, j] - 1] = coords_new[nodes[u - 1, j] - 1]
+    return nodes, coords_new, den_under, den_above
