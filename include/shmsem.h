@@ -86,7 +86,9 @@ typedef struct {
   double g33, e31, e32;
   double h;                /* laminate thickness h (voltage lever arm, blow-up guard 10*h) */
   int32_t frm_int;         /* frame interval in steps, 0 = no frames */
-  int32_t frame_dof;       /* 1..5: velocity component stored in frames (5 = w) */
+  int32_t frame_dof;       /* 0 = all DOF components, 1..5: one component (5 = w) */
+  int32_t frame_kind;      /* field_variable: 0 velocity, 1 displacement, 2 acceleration,
+                              3 all three (main_flat_shell.m:765-885) */
 } shm_run;
 
 typedef struct {
@@ -111,7 +113,8 @@ const char *shm_last_error(const shm_plan *plan);
  *   st      [nscen][nft]            excitation samples st(nn) (Hanning_signal.m)
  *   displ   [nscen][nft x n_out]    column-major per scenario (displ, :926)
  *   voltage [nscen][nft x n_sens]   column-major per scenario (voltage, :925)
- *   frames  [nscen][nframes x nnode] velocity frames, frame-major (V?_frame<c>)
+ *   frames  [nscen][nframes][nfields][nnode] frame fields ({U,V,A}{x,Fix,y,Fiy,z}_frame<c>):
+ *           kind-major (displacement, velocity, acceleration) then DOF order
  * Any output pointer may be NULL.  `stream` is a cudaStream_t or NULL. */
 shm_status shm_forward(shm_plan *plan, const double *st, double *displ, double *voltage,
                        double *frames, void *stream);
@@ -135,8 +138,9 @@ shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
 
 /* Plan facts: [0] total nodes, [1] total elements, [2] total DOF, [3] path
  * used (1 general, 2 structured), [4] precision, [5] frames per scenario,
- * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task. */
-shm_status shm_plan_info(const shm_plan *plan, int64_t *info9);
+ * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task,
+ * [9] fields per frame. */
+shm_status shm_plan_info(const shm_plan *plan, int64_t *info10);
 
 /* 3D solid (src/models/solid3D/main_spec3Dcuda_global_cpu_gpu3_wave_sens_opt_single_PCT_mat.m):
  * hexahedral spectral elements of 6 x 6 x 3 nodes, 3 DOF per node (u, v, w;
@@ -163,7 +167,7 @@ typedef struct {
 /* Creates a 3D-solid plan; shm_forward, shm_reset, shm_set_signal,
  * shm_advance, shm_read_outputs, shm_time_steps, shm_get_state (3 values per
  * node), shm_set_state, shm_mass and shm_plan_destroy accept it.  shm_run's
- * force_dof/out_dof use the 3-DOF numbering, frame_dof is 1..3, PZT sensor
+ * force_dof/out_dof use the 3-DOF numbering, frame_dof is 0 (all) or 1..3, PZT sensor
  * fields are ignored. */
 shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh *meshes, const shm_solid_material *mats,
                                  const shm_run *runs, const shm_options *opt, shm_plan **out);
@@ -216,6 +220,43 @@ shm_status shm_mass(shm_plan *plan, double *mg);
 shm_status shm_stiffness_static(int32_t fen, int32_t nnode, const int32_t *nodes, const double *coords,
                                 const double *lam, int32_t basket_rows, const int32_t *I_G, const int32_t *I_L,
                                 const double *U, double *F, void *stream);
+
+/* Wavefield frames on a uniform grid, spec2meshgrid_flat_shell.m:55-583.
+ * A grid holds, for nx x ny points spanning the mesh's bounding box inset by
+ * 1e-8 m (point p = iy + ny*ix, meshgrid order), the owner element among
+ * elements 0..fen_search-1 and the local coordinates (ksi, eta) after the
+ * reference's three Newton steps.  fen_search = fen minus the elements
+ * appended above a delamination (the reference searches 1..fen-|den_above|).
+ * remap [nnode] (1-based, or NULL) names the node whose value is read in
+ * place of each node: shell_surface 'top' over a delamination reads the
+ * den_above copy for every den_under node (U(nodes_under) = U(nodes_above)).
+ * device < 0 builds the set-up on the host only (shm_grid_points works, the
+ * interpolation calls return SHM_ERR_STATE). */
+typedef struct shm_grid shm_grid;
+shm_status shm_grid_create(const shm_mesh *mesh, int32_t fen_search, const int32_t *remap, int32_t nx,
+                           int32_t ny, int32_t device, shm_grid **out);
+shm_status shm_grid_destroy(shm_grid *grid);
+const char *shm_grid_last_error(const shm_grid *grid);
+/* Set-up results, each [nx*ny] (any pointer may be NULL); owner is 0-based;
+ * max_err = max distance between a point and its mapped (ksi, eta) (:264-266). */
+shm_status shm_grid_points(const shm_grid *grid, double *xp, double *yp, int32_t *owner, double *ksi,
+                           double *eta, double *max_err);
+/* Data [nframes][nx*ny] of motion 1..9 (flat_shell_variable_names.m:8-17:
+ * 1 x, 2 y, 3 z, 4 phi_x, 5 phi_y, 6 x + s phi_x, 7 y + s phi_y,
+ * 8 |in-plane|, 9 |total|, s = +h/2 surface 0 'top', -h/2 surface 1 'bottom')
+ * from host frames [nframes][nfields][nnode]; dof_field[5] gives the field
+ * index of u, phi_x, v, phi_y, w (-1 = absent). */
+shm_status shm_grid_interpolate(shm_grid *grid, const double *frames, int32_t nframes, int32_t nfields,
+                                const int32_t *dof_field, int32_t motion, int32_t surface, double h,
+                                double *data, void *stream);
+/* The same from the device-resident frames of scenario `scen` of a plan
+ * (field_variable kind: 0 velocity, 1 displacement, 2 acceleration), with no
+ * host round trip of the frames; data [nframes][nx*ny] on the host. */
+shm_status shm_grid_interpolate_plan(shm_grid *grid, shm_plan *plan, int32_t scen, int32_t kind,
+                                     int32_t motion, int32_t surface, double h, double *data, void *stream);
+/* Device time (ms, CUDA events) of one interpolation of all the plan's frames. */
+shm_status shm_grid_time(shm_grid *grid, shm_plan *plan, int32_t scen, int32_t kind, int32_t motion,
+                         int32_t surface, double h, int32_t reps, float *ms);
 
 #ifdef __cplusplus
 }

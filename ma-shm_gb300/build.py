@@ -13,9 +13,10 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libshmsem.so")
-SOURCES = [os.path.join(PKG_DIR, "csrc", f) for f in ("shmsem.cu", "static_stiffness.cu")]
+SOURCES = [os.path.join(PKG_DIR, "csrc", f) for f in ("shmsem.cu", "static_stiffness.cu", "wavefield.cu")]
 HEADERS = [os.path.join(PKG_DIR, "csrc", f) for f in ("shell_element.cuh", "shell_structured.cuh",
-                                                       "shell_structured_f32.cuh", "solid_element.cuh")] + [
+                                                       "shell_structured_f32.cuh", "solid_element.cuh",
+                                                       "internal.h")] + [
     os.path.join(REPO_DIR, "include", "shmsem.h")]
 
 NVCC_FLAGS = [

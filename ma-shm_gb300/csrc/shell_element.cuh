@@ -46,6 +46,30 @@ template <typename T> __device__ __forceinline__ T Wg(int r);
 template <> __device__ __forceinline__ double Wg<double>(int r) { return c_w64[r]; }
 template <> __device__ __forceinline__ float Wg<float>(int r) { return c_w32[r]; }
 
+// Wavefield frames (main_flat_shell.m:765-885).  Every frm_int steps the
+// displacement u_n (kind 0), the velocity a1*(u_{n+1} - u_{n-1}) (kind 1)
+// and/or the acceleration a0*(u_{n-1} - 2 u_n + u_{n+1}) (kind 2) of the
+// selected DOF components are stored as fields [frame][field][node_pad];
+// slot[kind*5 + dof] is the field index of (kind, dof) or -1.  Frame c
+// (0-based) is taken at loop index nn = (c + fc0) * frm_int, fc0 being the
+// first multiple of frm_int at or after the loop's first index.
+struct FrameSpec {
+  int frm_int, nframes, nfields, fc0;
+  signed char slot[15];
+};
+
+template <typename T>
+__device__ __forceinline__ void store_frame(const FrameSpec& fs, T* __restrict__ frames, int64_t npad,
+                                            int64_t node, int f, int nn, T u, T uo, T un, T a0, T a1) {
+  const int fc = nn / fs.frm_int - fs.fc0;
+  if (fc < 0 || fc >= fs.nframes) return;
+  T* base = frames + (int64_t)fc * fs.nfields * npad + node;
+  const int sU = fs.slot[f], sV = fs.slot[5 + f], sA = fs.slot[10 + f];
+  if (sU >= 0) base[sU * npad] = u;
+  if (sV >= 0) base[sV * npad] = a1 * (un - uo);
+  if (sA >= 0) base[sA * npad] = a0 * (uo - T(2) * u + un);
+}
+
 // Laminate coefficients of one element (composite_plate*.m outputs).
 template <typename T> struct Lam {
   T a11, a12, a16, a22, a26, a66, a44, a45, a55;

@@ -58,9 +58,9 @@ template <typename T> struct StructArgs {
   double* displ;
   double* vsum;
   SensorConst<T> sc;
-  int frm_int, frame_field, nframes;
+  FrameSpec fs;
   T* frames;
-  T a1, blowup;
+  T a0, a1, blowup;
   int* flag;
   const int* d_base;
 };
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
   const int q = lane % EW;  // element within the strip
   T* xs = sm + lane * ELEM_STRIDE;
   T* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
-  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false;
 
@@ -232,10 +232,7 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
           const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F);
           prev[f * a.nnode_pad + node] = un;
           if (frame) {
-            if (f == a.frame_field) {
-              const int fc = nn / a.frm_int - 1;
-              if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + node] = a.a1 * (un - uo);
-            }
+            store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
             if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
           }
         }

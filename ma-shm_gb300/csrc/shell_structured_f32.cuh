@@ -86,9 +86,9 @@ struct F32Args {
   double* displ;
   double* vsum;
   SensorConst<float> sc;
-  int frm_int, frame_field, nframes;
+  FrameSpec fs;
   float* frames;
-  float a1, blowup;
+  float a0, a1, blowup;
   int* flag;
   const int* d_base;
 };
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   const int q = lane % EW;
   float* xs = sm + lane * ELEM_STRIDE;
   float* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
-  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false;
   // owned band entries this thread updates: (group, logical row, owned column)
@@ -483,10 +483,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
           prev[f * a.nnode_pad + node] = un;
           if (frame) {
-            if (f == a.frame_field) {
-              const int fc = nn / a.frm_int - 1;
-              if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + node] = a.a1 * (un - uo);
-            }
+            store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
             if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
           }
         }

@@ -23,6 +23,7 @@
 
 #include "shmsem.h"
 #include "shell_element.cuh"
+#include "internal.h"
 
 using namespace shm;
 
@@ -64,9 +65,9 @@ template <typename T> struct GenArgs {
   double* vsum;                   // [nslot][nft]
   SensorConst<T> sc;
   // frames
-  int frm_int, frame_field, nframes;
-  T* frames;                      // [nframes][nnode_pad]
-  T a1;
+  FrameSpec fs;
+  T* frames;                      // [nframes][nfields][nnode_pad]
+  T a0, a1;
   T blowup;                       // 10*h
   int* flag;
   const int* d_base;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
     for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
   }
   const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
-  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   bool bad = false;
 #pragma unroll
   for (int f = 0; f < 5; ++f) {
@@ -271,10 +272,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
     const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
     prev[f * a.nnode_pad + g] = un;
     if (frame) {
-      if (f == a.frame_field) {
-        const int fc = nn / a.frm_int - 1;
-        if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + g] = a.a1 * (un - uo);
-      }
+      store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
       if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
     }
   }
@@ -362,7 +360,8 @@ struct shm_plan {
   std::vector<int64_t> node_off, elem_off;
   std::vector<int> out_off, sens_off, nout_s, nsens_s;
   int nout = 0, nsens = 0, nslot = 0, nforce = 0;
-  int frm_int = 0, frame_field = 4, nframes = 0;
+  int frm_int = 0, nframes = 0, nfields = 0;
+  FrameSpec fspec{};
   std::vector<double> mass;  // [nnode][5] host copy (interleaved)
   // device memory
   std::vector<void*> allocs;
@@ -403,6 +402,37 @@ static shm_status bad(shm_plan* p, const std::string& m) {
   return SHM_ERR_BAD_ARG;
 }
 
+// Frame selection of a run (main_flat_shell.m:765-885, field_variable):
+// frame_kind 0 velocity, 1 displacement, 2 acceleration, 3 all three;
+// frame_dof 0 = every DOF component, else the one component 1..ndof.
+// Fields are ordered kind-major (displacement, velocity, acceleration), then
+// by DOF (u, phi_x, v, phi_y, w), the order of the reference's frame files.
+static shm_status set_frames(shm_plan* p, const shm_run& r, int ndof) {
+  FrameSpec& fs = p->fspec;
+  fs = FrameSpec{};
+  for (int i = 0; i < 15; ++i) fs.slot[i] = -1;
+  p->frm_int = r.frm_int > 0 ? r.frm_int : 0;
+  p->nframes = p->nfields = 0;
+  if (p->frm_int == 0) return SHM_OK;
+  if (r.frame_dof < 0 || r.frame_dof > ndof) return bad(p, "frame_dof must be 0 (all) or 1..ndof");
+  if (r.frame_kind < 0 || r.frame_kind > 3) return bad(p, "frame_kind must be 0..3");
+  static const int kind_of[3] = {1, 0, 2};   // API kind -> displacement/velocity/acceleration slot
+  int nf = 0;
+  for (int k = 0; k < 3; ++k) {
+    if (r.frame_kind != 3 && kind_of[r.frame_kind] != k) continue;
+    for (int f = 0; f < ndof; ++f)
+      if (r.frame_dof == 0 || r.frame_dof - 1 == f) fs.slot[k * 5 + f] = (signed char)nf++;
+  }
+  const int nf0 = r.nn_first > 0 ? r.nn_first : 1;
+  fs.fc0 = (nf0 + p->frm_int - 1) / p->frm_int;
+  p->nfields = nf;
+  p->nframes = std::max(0, r.nft / p->frm_int - fs.fc0 + 1);
+  fs.frm_int = p->frm_int;
+  fs.nframes = p->nframes;
+  fs.nfields = nf;
+  return SHM_OK;
+}
+
 template <typename X>
 static shm_status dalloc(shm_plan* p, X** out, size_t count) {
   void* q = nullptr;
@@ -428,7 +458,7 @@ static shm_status upload(shm_plan* p, X** out, const std::vector<X>& v) {
 
 // GLL nodes/weights (Newton on P'_{n-1} from Chebyshev-Lobatto guesses) and
 // the Lagrange derivative matrix by barycentric weights.
-static void gll_setup(int n, std::vector<double>& x, std::vector<double>& w, std::vector<double>& D) {
+void shm::gll_setup(int n, std::vector<double>& x, std::vector<double>& w, std::vector<double>& D) {
   x.assign(n, 0.0);
   w.assign(n, 0.0);
   const int N = n - 1;
@@ -585,10 +615,9 @@ template <typename T> static GenArgs<T> make_args(shm_plan* p) {
   a.esens = p->esens;
   a.vsum = p->vsum;
   fill_sc(p, a.sc);
-  a.frm_int = p->frm_int;
-  a.frame_field = p->frame_field;
-  a.nframes = p->nframes;
+  a.fs = p->fspec;
   a.frames = (T*)p->frames;
+  a.a0 = (T)p->a0;
   a.a1 = (T)p->a1;
   a.blowup = (T)p->blowup;
   a.flag = p->flag;
@@ -897,10 +926,9 @@ static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s
   a.displ = p->displ;
   a.vsum = p->vsum;
   fill_sc(p, a.sc);
-  a.frm_int = p->frm_int;
-  a.frame_field = p->frame_field;
-  a.nframes = p->nframes;
+  a.fs = p->fspec;
   a.frames = (float*)p->frames;
+  a.a0 = (float)p->a0;
   a.a1 = (float)p->a1;
   a.blowup = (float)p->blowup;
   a.flag = p->flag;
@@ -954,10 +982,9 @@ static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.displ = p->displ;
   a.vsum = p->vsum;
   fill_sc(p, a.sc);
-  a.frm_int = p->frm_int;
-  a.frame_field = p->frame_field;
-  a.nframes = p->nframes;
+  a.fs = p->fspec;
   a.frames = (T*)p->frames;
+  a.a0 = (T)p->a0;
   a.a1 = (T)p->a1;
   a.blowup = (T)p->blowup;
   a.flag = p->flag;
@@ -994,7 +1021,7 @@ static shm_status build_device(shm_plan* p, const std::vector<int>& conn, const 
   if ((s = dalloc(p, &ua, (size_t)5 * p->nnode_pad)) != SHM_OK) return s;
   if ((s = dalloc(p, &ub, (size_t)5 * p->nnode_pad)) != SHM_OK) return s;
   if ((s = dalloc(p, &f2, (size_t)5 * p->plane)) != SHM_OK) return s;
-  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nnode_pad)) != SHM_OK) return s;
+  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nfields * p->nnode_pad)) != SHM_OK) return s;
   p->geo = g;
   p->ekeep = k;
   p->mat = m;
@@ -1046,12 +1073,7 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
     p->k1[f] = (p->a0 - p->a1 * eta[f]) / den;
     p->k2[f] = 1.0 / den;
   }
-  p->frm_int = r0.frm_int > 0 ? r0.frm_int : 0;
-  if (p->frm_int > 0) {
-    if (r0.frame_dof < 1 || r0.frame_dof > 5) return bad(p, "frame_dof must be 1..5");
-    p->frame_field = r0.frame_dof - 1;
-    p->nframes = r0.nft / p->frm_int;
-  }
+  if (set_frames(p, r0, 5) != SHM_OK) return SHM_ERR_BAD_ARG;
   p->blowup = 10.0 * r0.h;
   if (!(r0.h > 0)) p->blowup = INFINITY;
 
@@ -1356,7 +1378,7 @@ extern "C" shm_status shm_reset(shm_plan* p) {
   const size_t ts = p->prec == 64 ? 8 : 4;
   CKP(p, cudaMemsetAsync(p->UA, 0, ts * p->nf * p->nnode_pad, s));
   CKP(p, cudaMemsetAsync(p->UB, 0, ts * p->nf * p->nnode_pad, s));
-  if (p->frames) CKP(p, cudaMemsetAsync(p->frames, 0, ts * p->nframes * p->nnode_pad, s));
+  if (p->frames) CKP(p, cudaMemsetAsync(p->frames, 0, ts * p->nframes * p->nfields * p->nnode_pad, s));
   CKP(p, cudaMemsetAsync(p->displ, 0, sizeof(double) * std::max(p->nout, 1) * p->nft, s));
   CKP(p, cudaMemsetAsync(p->vsum, 0, sizeof(double) * std::max(p->nslot, 1) * p->nft, s));
   CKP(p, cudaMemsetAsync(p->flag, 0, 4, s));
@@ -1459,12 +1481,16 @@ extern "C" shm_status shm_time_steps(shm_plan* p, int32_t nsteps, float* ms) {
 
 template <typename T>
 static void to_host_frames(const std::vector<T>& dev, shm_plan* p, double* frames) {
-  // device [nframes][nnode_pad] over all scenarios -> [nscen][nframes][nnode_s]
+  // device [nframes][nfields][nnode_pad] over all scenarios
+  //   -> [nscen][nframes][nfields][nnode_s]
   double* o = frames;
   for (int s = 0; s < p->nscen; ++s) {
     const int64_t n0 = p->node_off[s], nn = p->node_off[s + 1] - n0;
     for (int c = 0; c < p->nframes; ++c)
-      for (int64_t g = 0; g < nn; ++g) *o++ = (double)dev[(size_t)c * p->nnode_pad + n0 + g];
+      for (int f = 0; f < p->nfields; ++f) {
+        const T* src = dev.data() + ((size_t)c * p->nfields + f) * p->nnode_pad + n0;
+        for (int64_t g = 0; g < nn; ++g) *o++ = (double)src[g];
+      }
   }
 }
 
@@ -1481,7 +1507,7 @@ extern "C" shm_status shm_read_outputs(shm_plan* p, double* displ, double* volta
     CKP(p, cudaMemcpyAsync(voltage, p->volt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   }
   if (frames && p->nframes > 0) {
-    const size_t cnt = (size_t)p->nframes * p->nnode_pad;
+    const size_t cnt = (size_t)p->nframes * p->nfields * p->nnode_pad;
     if (p->prec == 64) {
       std::vector<double> h(cnt);
       CKP(p, cudaMemcpyAsync(h.data(), p->frames, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
@@ -1613,6 +1639,7 @@ extern "C" shm_status shm_plan_info(const shm_plan* p, int64_t* info) {
   info[6] = p->path == 2 ? 1 : 2;
   info[7] = p->path == 2 ? p->sp.tile : 0;
   info[8] = p->path == 2 ? p->sp.H : 0;
+  info[9] = p->nfields;
   return SHM_OK;
 }
 
@@ -1765,7 +1792,7 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   a.asig = p->asig;
   a.seg = seg;
   a.grad = p->grad;
-  a.frm_int = 0;
+  a.fs.frm_int = 0;
   a.nout = 0;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
@@ -1859,10 +1886,9 @@ static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.out_node = p->out_node;
   a.out_field = p->out_field;
   a.displ = p->displ;
-  a.frm_int = p->frm_int;
-  a.frame_field = p->frame_field;
-  a.nframes = p->nframes;
+  a.fs = p->fspec;
   a.frames = (T*)p->frames;
+  a.a0 = (T)p->a0;
   a.a1 = (T)p->a1;
   a.blowup = (T)p->blowup;
   a.flag = p->flag;
@@ -1893,7 +1919,7 @@ static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const 
   if ((s = dalloc(p, &ua, (size_t)3 * p->nnode_pad)) != SHM_OK) return s;
   if ((s = dalloc(p, &ub, (size_t)3 * p->nnode_pad)) != SHM_OK) return s;
   if ((s = dalloc(p, &f2, (size_t)3 * p->plane)) != SHM_OK) return s;
-  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nnode_pad)) != SHM_OK) return s;
+  if (p->nframes > 0 && (s = dalloc(p, &fr, (size_t)p->nframes * p->nfields * p->nnode_pad)) != SHM_OK) return s;
   p->geo = g;
   p->ekeep = k;
   p->mat = m;
@@ -1945,12 +1971,7 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
     p->k1[f] = (p->a0 - p->a1 * eta[f]) / den;
     p->k2[f] = 1.0 / den;
   }
-  p->frm_int = r0.frm_int > 0 ? r0.frm_int : 0;
-  if (p->frm_int > 0) {
-    if (r0.frame_dof < 1 || r0.frame_dof > 3) return bad(p, "frame_dof must be 1..3 for solids");
-    p->frame_field = r0.frame_dof - 1;
-    p->nframes = r0.nft / p->frm_int;
-  }
+  if (set_frames(p, r0, 3) != SHM_OK) return SHM_ERR_BAD_ARG;
   p->blowup = INFINITY;
   p->node_off.assign(nscen + 1, 0);
   p->elem_off.assign(nscen + 1, 0);
@@ -2136,4 +2157,21 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
   if ((st = dalloc(p, &p->d_base, 4)) != SHM_OK) return st;
   CKP(p, cudaDeviceSynchronize());
   return shm_reset(p);
+}
+
+shm_status shm::plan_frames_view(shm_plan* p, int scen, FramesView* v) {
+  if (!p || !v || scen < 0 || scen >= p->nscen) return SHM_ERR_BAD_ARG;
+  v->frames = p->frames;
+  v->prec = p->prec;
+  v->nnode_pad = p->nnode_pad;
+  v->node0 = p->node_off[scen];
+  v->nnode = p->node_off[scen + 1] - p->node_off[scen];
+  v->nframes = p->nframes;
+  v->nfields = p->nfields;
+  for (int i = 0; i < 15; ++i) v->slot[i] = p->fspec.slot[i];
+  v->device = p->device;
+  v->kind = p->kind;
+  v->ndof = p->nf;
+  v->stream = (void*)p->stream;
+  return SHM_OK;
 }

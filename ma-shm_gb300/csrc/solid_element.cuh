@@ -53,9 +53,9 @@ template <typename T> struct SolidArgs {
   const int* __restrict__ out_node;
   const int* __restrict__ out_field;
   double* displ;
-  int frm_int, frame_field, nframes;
+  FrameSpec fs;
   T* frames;
-  T a1, blowup;
+  T a0, a1, blowup;
   int* flag;
   const int* d_base;
 };
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
     for (int f = 0; f < 3; ++f) F[f] += a.F2[f * a.plane + slot];
   }
   const T im = a.minv[g];
-  const bool frame = a.frm_int > 0 && (nn % a.frm_int) == 0;
+  const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   bool bad = false;
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
@@ -174,10 +174,7 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
     const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
     prev[f * a.nnode_pad + g] = un;
     if (frame) {
-      if (f == a.frame_field) {
-        const int fc = nn / a.frm_int - 1;
-        if (fc < a.nframes) a.frames[(int64_t)fc * a.nnode_pad + g] = a.a1 * (un - uo);
-      }
+      store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
       if (!isfinite(un)) bad = true;
     }
   }

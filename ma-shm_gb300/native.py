@@ -40,7 +40,7 @@ class ShmRun(C.Structure):
                 ("n_sens", C.c_int32), ("sens_ptr", I32P), ("sens_el", I32P),
                 ("pzt_thickness", C.c_double), ("g33", C.c_double), ("e31", C.c_double),
                 ("e32", C.c_double), ("h", C.c_double),
-                ("frm_int", C.c_int32), ("frame_dof", C.c_int32)]
+                ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("frame_kind", C.c_int32)]
 
 
 class ShmSolidMesh(C.Structure):
@@ -89,6 +89,17 @@ SIGNATURES = {
                                C.POINTER(C.c_float)]),
     "shm_stiffness_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "shm_grid_create": (C.c_int, [C.POINTER(ShmMesh), C.c_int32, I32P, C.c_int32, C.c_int32, C.c_int32,
+                                  C.POINTER(C.c_void_p)]),
+    "shm_grid_destroy": (C.c_int, [C.c_void_p]),
+    "shm_grid_last_error": (C.c_char_p, [C.c_void_p]),
+    "shm_grid_points": (C.c_int, [C.c_void_p, F64P, F64P, I32P, F64P, F64P, F64P]),
+    "shm_grid_interpolate": (C.c_int, [C.c_void_p, F64P, C.c_int32, C.c_int32, I32P, C.c_int32, C.c_int32,
+                                       C.c_double, F64P, C.c_void_p]),
+    "shm_grid_interpolate_plan": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                            C.c_double, F64P, C.c_void_p]),
+    "shm_grid_time": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                C.c_int32, C.POINTER(C.c_float)]),
 }
 
 

@@ -46,7 +46,8 @@ class RunConfig:
     eta_z: float = 0.0
     h: float = 0.0
     frm_int: int = 0
-    frame_dof: int = 5
+    frame_dof: int = 5               # 0 = all five components, else 1..5 (5 = w)
+    frame_kind: int = 0              # 0 velocity, 1 displacement, 2 acceleration, 3 all three
 
 
 class Plan:
@@ -80,10 +81,11 @@ class Plan:
         self.nf = 5
 
     def _refresh_info(self):
-        info = (C.c_int64 * 9)()
+        info = (C.c_int64 * 10)()
         self.lib.shm_plan_info(self.handle, info)
         self.info = dict(nnode=info[0], fen=info[1], ndof=info[2], path=info[3], precision=info[4],
-                         nframes=info[5], launches_per_step=info[6], tile=info[7], rows_per_block=info[8])
+                         nframes=info[5], launches_per_step=info[6], tile=info[7], rows_per_block=info[8],
+                         nfields=info[9])
 
     def autotune(self, steps: int = 20):
         """Pick the structured kernel's lane-group width and rows per task by timing."""
@@ -156,7 +158,7 @@ class Plan:
         else:
             r.n_sens = 0
         r.h = run.h
-        r.frm_int, r.frame_dof = run.frm_int, run.frame_dof
+        r.frm_int, r.frame_dof, r.frame_kind = run.frm_int, run.frame_dof, run.frame_kind
 
     # ------------------------------------------------------------------
     def _check(self, st):
@@ -184,7 +186,8 @@ class Plan:
         displ = np.zeros(max(nout, 1) * self.nft)
         volt = np.zeros(max(nsens, 1) * self.nft)
         nfr = self.info["nframes"]
-        frames = np.zeros(max(nfr * self.info["nnode"], 1)) if (want_frames and nfr) else None
+        frames = (np.zeros(max(nfr * self.info["nfields"] * self.info["nnode"], 1))
+                  if (want_frames and nfr) else None)
         self._check(self.lib.shm_forward(self.handle, native.ptr(st), native.ptr(displ), native.ptr(volt),
                                          native.ptr(frames), None))
         return self._split(displ, volt, frames)
@@ -199,9 +202,9 @@ class Plan:
             v = volt[s_ * self.nft:(s_ + ns) * self.nft].reshape(ns, self.nft).T.copy()
             res = dict(displ=d, voltage=v)
             if frames is not None:
-                nfr = self.info["nframes"]
-                res["frames"] = frames[fo:fo + nfr * nnode].reshape(nfr, nnode).copy()
-                fo += nfr * nnode
+                nfr, nfl = self.info["nframes"], self.info["nfields"]
+                res["frames"] = frames[fo:fo + nfr * nfl * nnode].reshape(nfr, nfl, nnode).copy()
+                fo += nfr * nfl * nnode
             out.append(res)
             o += no
             s_ += ns
@@ -228,7 +231,8 @@ class Plan:
         displ = np.zeros(max(nout, 1) * self.nft)
         volt = np.zeros(max(nsens, 1) * self.nft)
         nfr = self.info["nframes"]
-        frames = np.zeros(max(nfr * self.info["nnode"], 1)) if (want_frames and nfr) else None
+        frames = (np.zeros(max(nfr * self.info["nfields"] * self.info["nnode"], 1))
+                  if (want_frames and nfr) else None)
         self._check(self.lib.shm_read_outputs(self.handle, native.ptr(displ), native.ptr(volt),
                                               native.ptr(frames), None))
         return self._split(displ, volt, frames)
@@ -304,7 +308,7 @@ class SolidPlan(Plan):
             r.n_out, r.out_dof = len(od), native.ptr(od, native.I32P)
             r.n_sens = 0
             r.h = run.h
-            r.frm_int, r.frame_dof = run.frm_int, run.frame_dof
+            r.frm_int, r.frame_dof, r.frame_kind = run.frm_int, run.frame_dof, run.frame_kind
         opt = native.ShmOptions(precision, 1, steps_per_graph, 0, device, 0)
         handle = C.c_void_p()
         st = self.lib.shm_solid_plan_create(n, meshes, mats, runs, C.byref(opt), C.byref(handle))
@@ -346,8 +350,9 @@ def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", outp
     variant: 'main_flat_shell' (dt = tt/nft, loop nn = 2..nft, force at the
     plate centre) or 'force_excit_c' (dt = tt/(nft-1), nn = 1..nft, force at
     ``force_coords``, outputs at ``output_coords``).
-    Writes displ<test_case>.mat, time<test_case>.mat and velocity frames
-    V{x,Fix,y,Fiy,z}_frame<c>.mat (field_variable 'velocity' only) into
+    Writes displ<test_case>.mat, time<test_case>.mat and the wavefield frames
+    {U,V,A}{x,Fix,y,Fiy,z}_frame<c>.mat of field_variable 'displacement',
+    'velocity', 'acceleration' or 'all' (main_flat_shell.m:806-885) into
     output_name; returns t_frames.
     """
     if mode != "gpu":
@@ -384,14 +389,16 @@ def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", outp
     fv = inputs.get("field_variable", "velocity")
     sc = Scenario(mesh=mesh, mat_table=table, force_dof=np.array([5 * force_node], np.int32),
                   force_val=np.array([inputs["V0"]]), out_dof=5 * np.array(out_nodes, np.int32), signal=st)
+    kinds = {"velocity": 0, "displacement": 1, "acceleration": 2, "all": 3}
+    if fv not in kinds:
+        raise ValueError(f"field_variable must be one of {sorted(kinds)}")
     run = RunConfig(dt=dt, nft=nft, nn_first=nn_first, eta_xy=inputs.get("etad_xy", 0.0),
-                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int if fv == "velocity" else 0,
-                    frame_dof=5)
+                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int, frame_dof=0, frame_kind=kinds[fv])
     os.makedirs(output_name, exist_ok=True)
     tic = time.perf_counter()
     plan = Plan([sc], run, precision=precision)
     try:
-        res = plan.forward(want_frames=(fv == "velocity" and frm_int > 0))[0]
+        res = plan.forward(want_frames=frm_int > 0)[0]
     finally:
         plan.close()
     elapsed = time.perf_counter() - tic
@@ -402,10 +409,11 @@ def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", outp
              "TotalNofNodes": n_nodes, "t": t})
     t_frames = np.zeros(nframes)
     if "frames" in res:
-        # frame c at loop index nn = c*frm_int; only the w velocity is computed
-        # on the device (frame_dof=5), the other components are written as in
-        # the reference only when requested through frame_dof
-        for c in range(res["frames"].shape[0]):
-            t_frames[c] = t[(c + 1) * frm_int - 1]
-            savemat(os.path.join(output_name, f"Vz_frame{c + 1}.mat"), {"Vz": res["frames"][c][:, None]})
+        names = [p + c for p in {"displacement": "U", "velocity": "V", "acceleration": "A",
+                                 "all": "UVA"}[fv] for c in ("x", "Fix", "y", "Fiy", "z")]
+        first = (nn_first + frm_int - 1) // frm_int
+        for c in range(min(res["frames"].shape[0], nframes)):
+            t_frames[c] = t[(c + first) * frm_int - 1]
+            for name, fld in zip(names, res["frames"][c]):
+                savemat(os.path.join(output_name, f"{name}_frame{c + 1}.mat"), {name: fld[:, None]})
     return t_frames

@@ -38,7 +38,8 @@ class OracleArgs(C.Structure):
                 ("nsens", C.c_int32), ("sens_ptr", I32P), ("sens_el", I32P),
                 ("pzt_thickness", C.c_double), ("g33", C.c_double), ("e31", C.c_double), ("e32", C.c_double),
                 ("h", C.c_double), ("voltage", F64P),
-                ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("nframes_max", C.c_int32),
+                ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("frame_kind", C.c_int32),
+                ("nframes_max", C.c_int32),
                 ("frames", F64P), ("t_frames_step", F64P), ("nthreads", C.c_int32),
                 ("U", F64P), ("uold", F64P), ("frames_written", C.c_int32), ("diverged_at", C.c_int32)]
 
@@ -159,7 +160,7 @@ class OracleProblem:
         return F
 
     def run(self, dt, nft, st, nn_first=2, eta_xy=0.0, eta_z=0.0, force_dof=(), force_val=(), out_dof=(),
-            sensors=(), pzt=None, h=0.0, frm_int=0, frame_dof=5, U0=None, uold0=None, nthreads=0,
+            sensors=(), pzt=None, h=0.0, frm_int=0, frame_dof=5, frame_kind=0, U0=None, uold0=None, nthreads=0,
             nn_last=None):
         keep = []
         A = self._args(keep)
@@ -189,10 +190,12 @@ class OracleProblem:
         A.h = h
         voltage = np.zeros(max(len(sensors), 1) * nft)
         A.voltage = _p(voltage)
-        nfr = nft // frm_int if frm_int else 0
-        frames = np.zeros(max(nfr, 1) * self.nnode)
+        # frames at every nn in [nn_first, nft] with nn % frm_int == 0
+        nfr = (nft // frm_int - (nn_first + frm_int - 1) // frm_int + 1) if frm_int else 0
+        nfld = (3 if frame_kind == 3 else 1) * (5 if frame_dof == 0 else 1)
+        frames = np.zeros(max(nfr * nfld, 1) * self.nnode)
         tfs = np.zeros(max(nfr, 1))
-        A.frm_int, A.frame_dof, A.nframes_max = frm_int, frame_dof, nfr
+        A.frm_int, A.frame_dof, A.frame_kind, A.nframes_max = frm_int, frame_dof, frame_kind, nfr
         A.frames, A.t_frames_step = _p(frames), _p(tfs)
         A.nthreads = nthreads
         U = np.zeros(self.ndof) if U0 is None else np.ascontiguousarray(U0, float).copy()
@@ -202,7 +205,7 @@ class OracleProblem:
         assert rc == 0
         return dict(displ=displ[:len(od) * nft].reshape(nft, len(od)) if len(od) else np.zeros((nft, 0)),
                     voltage=voltage[:len(sensors) * nft].reshape(nft, len(sensors)) if sensors else np.zeros((nft, 0)),
-                    frames=frames[:nfr * self.nnode].reshape(nfr, self.nnode), U=U, uold=Uo,
+                    frames=frames[:nfr * nfld * self.nnode].reshape(nfr, nfld, self.nnode), U=U, uold=Uo,
                     diverged_at=A.diverged_at, frames_written=A.frames_written)
 
 

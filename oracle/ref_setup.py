@@ -716,3 +716,184 @@ def split_delam_nodes_flat_shell(nodes, coords, den1, nx, ny, boundary_nodes):
         for j in range(nx * ny):
             coords_new[nodes[a - 1, j] - 1] = coords_new[nodes[u - 1, j] - 1]
     return nodes, coords_new, den_under, den_above
+
+
+# --------------------------------------------------------------------------
+# wavefield on a uniform grid
+# --------------------------------------------------------------------------
+
+
+def vandermonde2d(ksi, eta, nx, ny):
+    """``src/models/solid3D/Vandermonde2D.m``: V(r,c) = ksi(i2)^(j2-1) eta(i1)^(j1-1),
+    rows r over (eta point i1, ksi point i2), columns over (eta degree j1,
+    ksi degree j2), ksi fastest; Q = inv(V)."""
+    V = np.zeros((nx * ny, nx * ny))
+    r = 0
+    for i1 in range(ny):
+        for i2 in range(nx):
+            c = 0
+            for j1 in range(ny):
+                for j2 in range(nx):
+                    V[r, c] = ksi[i2] ** j2 * eta[i1] ** j1
+                    c += 1
+            r += 1
+    return np.linalg.inv(V)
+
+
+def shape2dp(nx, ny, Q, x, y):
+    """``src/models/solid3D/shape2Dp.m``: N = Q' f, f(c,:) = x^(j2-1) y^(j1-1)."""
+    f = np.zeros((nx * ny, len(x)))
+    c = 0
+    for j1 in range(ny):
+        for j2 in range(nx):
+            f[c] = x ** j2 * y ** j1
+            c += 1
+    return Q.T @ f
+
+
+def shape_derivatives2dp(nx, ny, Q, x, y):
+    """``src/models/solid3D/shape_derivatives2Dp.m`` (0 * x^-1 terms kept as
+    written: they are NaN at x = 0 exactly, as in MATLAB)."""
+    fx = np.zeros((nx * ny, len(x)))
+    fy = np.zeros((nx * ny, len(x)))
+    c = 0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for j1 in range(ny):
+            for j2 in range(nx):
+                fx[c] = (j2 * x ** (j2 - 1.0)) * y ** j1
+                fy[c] = x ** j2 * (j1 * y ** (j1 - 1.0))
+                c += 1
+    return Q.T @ fx, Q.T @ fy
+
+
+def _colon(a, d, b):
+    """MATLAB a:d:b as a + k*d, k = 0..floor((b-a)/d) (with a relative
+    tolerance on the count, as MATLAB's colon)."""
+    n = int(np.floor((b - a) / d + 1e-10)) + 1
+    return a + np.arange(n) * d
+
+
+def spec2meshgrid_flat_shell(nodes1, coords, Nx, Ny, fields, motion, shell_surface, h, den_under=(), den_above=(),
+                             shape_order=5):
+    """``src/models/flat_shell/flat_shell_engine/spec2meshgrid_flat_shell.m:55-583``.
+
+    fields: dict of the frame vectors the motion needs, each [nFrames, nnode]
+    ('x', 'Fix', 'y', 'Fiy', 'z' components of the chosen field_variable);
+    den_under/den_above: 0-based element lists of one delamination (or empty).
+    Returns (Data [Ny, Nx, nFrames] as the reference's, dict of set-up
+    intermediates: xp, yp, owner (0-based), ksi_p, eta_p, max_err).
+    The clamping at :268-271 comes after the shape functions are evaluated
+    and has no effect; it is not restated.
+    """
+    Eps = 1e-8
+    nodes1 = np.asarray(nodes1)
+    coords = np.asarray(coords, float)
+    n = shape_order + 1
+    NofElNodes = n * n
+    mc = np.array([1, n, n * n, n * n - n + 1]) - 1
+    fen = nodes1.shape[0]
+    if len(den_above):
+        fen = fen - len(den_above)          # 'top' and 'bottom' remove as many elements
+    ne = np.arange(fen)
+    L = coords[:, 0].max() - coords[:, 0].min() - 2 * Eps
+    xi = _colon(coords[:, 0].min() + Eps, L / (Nx - 1), coords[:, 0].max() - Eps)
+    B = coords[:, 1].max() - coords[:, 1].min() - 2 * Eps
+    yi = _colon(coords[:, 1].min() + Eps, B / (Ny - 1), coords[:, 1].max() - Eps)
+    XI, YI = np.meshgrid(xi, yi)
+    xp = XI.reshape(-1, order="F")
+    yp = YI.reshape(-1, order="F")
+    x = coords[nodes1[ne][:, mc] - 1, 0].T       # [4, fen]
+    y = coords[nodes1[ne][:, mc] - 1, 1].T
+    x21, x32, x43, x14 = x[1] - x[0], x[2] - x[1], x[3] - x[2], x[0] - x[3]
+    y21, y32, y43, y14 = y[1] - y[0], y[2] - y[1], y[3] - y[2], y[0] - y[3]
+    x1y21, y1x21 = x[0] * y21, y[0] * x21
+    x2y32, y2x32 = x[1] * y32, y[1] * x32
+    x3y43, y3x43 = x[2] * y43, y[2] * x43
+    x4y14, y4x14 = x[3] * y14, y[3] * x14
+    Pmin_x, Pmin_y, Pmax_x, Pmax_y = x.min(0), y.min(0), x.max(0), y.max(0)
+    owner = np.zeros(len(xp), dtype=np.int64)
+    for j in range(len(xp)):
+        Ibb = np.nonzero((xp[j] >= Pmin_x) & (xp[j] <= Pmax_x) & (yp[j] >= Pmin_y) & (yp[j] <= Pmax_y))[0]
+        if len(Ibb) == 1:
+            owner[j] = Ibb[0]
+        else:
+            d1 = (xp[j] * y21[Ibb] - x1y21[Ibb]) - (yp[j] * x21[Ibb] - y1x21[Ibb])
+            d2 = (xp[j] * y32[Ibb] - x2y32[Ibb]) - (yp[j] * x32[Ibb] - y2x32[Ibb])
+            d3 = (xp[j] * y43[Ibb] - x3y43[Ibb]) - (yp[j] * x43[Ibb] - y3x43[Ibb])
+            d4 = (xp[j] * y14[Ibb] - x4y14[Ibb]) - (yp[j] * x14[Ibb] - y4x14[Ibb])
+            neg = (d1 < 0) & (d2 < 0) & (d3 < 0) & (d4 < 0)
+            idx = np.nonzero(neg)[0]
+            owner[j] = Ibb[0] if len(idx) == 0 else Ibb[idx[0]]
+    ksi, _ = gll(n)
+    eta, _ = gll(n)
+    Ksi, Eta = np.meshgrid(ksi, eta)
+    Ksi = Ksi.T.reshape(-1, order="F")            # reshape(Ksi',1,[])
+    Eta = Eta.T.reshape(-1, order="F")
+    en = nodes1[owner]                             # [npts, 36]
+    x_0 = coords[en - 1, 0]
+    y_0 = coords[en - 1, 1]
+    point_no = np.argmin(np.sqrt((x_0 - xp[:, None]) ** 2 + (y_0 - yp[:, None]) ** 2), axis=1)
+    r = np.arange(len(xp))
+    x0, y0 = x_0[r, point_no], y_0[r, point_no]
+    ksi0, eta0 = Ksi[point_no], Eta[point_no]
+    # inverse Jacobian at the owner's first local node (<meshfile>_jacobians.mat)
+    Q1 = vandermonde(ksi)
+    Nprimx, Nprimy = shape2d_prim(n, n, Q1, Q1, ksi, eta)
+    jac = jacobians(nodes1, coords, Nprimx, Nprimy)
+    n1 = owner * NofElNodes
+    ksi_p = ksi0 + jac["invJ11"][n1] * (xp - x0) + jac["invJ12"][n1] * (yp - y0)
+    eta_p = eta0 + jac["invJ21"][n1] * (xp - x0) + jac["invJ22"][n1] * (yp - y0)
+    Q = vandermonde2d(ksi, eta, n, n)
+    N = shape2dp(n, n, Q, ksi_p, eta_p)            # [36, npts]
+    xe = x_0.T                                     # [36, npts]
+    ye = y_0.T
+    x1 = np.einsum("kp,kp->p", N, xe)
+    y1 = np.einsum("kp,kp->p", N, ye)
+    for _ in range(3):
+        ksi0, eta0, x0, y0 = ksi_p, eta_p, x1, y1
+        Npx, Npy = shape_derivatives2dp(n, n, Q, ksi0, eta0)
+        J11 = np.einsum("kp,kp->p", Npx, xe)
+        J12 = np.einsum("kp,kp->p", Npy, xe)
+        J21 = np.einsum("kp,kp->p", Npx, ye)
+        J22 = np.einsum("kp,kp->p", Npy, ye)
+        a = 1.0 / (J11 * J22 - J12 * J21)
+        ksi_p = ksi0 + (a * J22) * (xp - x0) + (a * (-J12)) * (yp - y0)
+        eta_p = eta0 + (a * (-J21)) * (xp - x0) + (a * J11) * (yp - y0)
+        N = shape2dp(n, n, Q, ksi_p, eta_p)
+        x1 = np.einsum("kp,kp->p", N, xe)
+        y1 = np.einsum("kp,kp->p", N, ye)
+    max_err = float(np.max(np.sqrt((xp - x1) ** 2 + (yp - y1) ** 2)))
+    # motion values per frame (:281-510)
+    s = h / 2 if shell_surface == "top" else -h / 2
+    F = {k: np.atleast_2d(np.asarray(v, float)) for k, v in fields.items()}
+    if motion == 1:
+        U = F["x"]
+    elif motion == 2:
+        U = F["y"]
+    elif motion == 3:
+        U = F["z"]
+    elif motion == 4:
+        U = F["Fix"]
+    elif motion == 5:
+        U = F["Fiy"]
+    elif motion == 6:
+        U = F["x"] + s * F["Fix"]
+    elif motion == 7:
+        U = F["y"] + s * F["Fiy"]
+    elif motion == 8:
+        U = np.sqrt((F["x"] + s * F["Fix"]) ** 2 + (F["y"] + s * F["Fiy"]) ** 2)
+    else:
+        U = np.sqrt((F["x"] + s * F["Fix"]) ** 2 + (F["y"] + s * F["Fiy"]) ** 2 + F["z"] ** 2)
+    U = U.copy()
+    if shell_surface == "top" and len(den_above):
+        nu = nodes1[np.asarray(den_under)].reshape(-1, order="F") - 1
+        na = nodes1[np.asarray(den_above)].reshape(-1, order="F") - 1
+        U[:, nu] = U[:, na]
+    if Nx != Ny:
+        raise ValueError("the reference stores reshape(ZI, Nx, Ny) into Data(Ny, Nx, :): Nx must equal Ny")
+    Data = np.zeros((Ny, Nx, U.shape[0]))
+    for f in range(U.shape[0]):
+        ZA = U[f][en - 1].T                         # [36, npts]
+        ZI = np.einsum("kp,kp->p", N, ZA)
+        Data[:, :, f] = ZI.reshape((Nx, Ny), order="F")
+    return Data, dict(xp=xp, yp=yp, owner=owner, ksi_p=ksi_p, eta_p=eta_p, max_err=max_err)

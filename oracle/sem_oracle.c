@@ -19,7 +19,8 @@
  *   update           F=-F+mg2.*U+Fa*st(nn)-mg.*uold+a1*cg.*uold;
  *                    unew=mg0.*F                                  :742-750
  *   outputs          displ(nn,:)=U(outputs)                       :752-764
- *   frames           v=a1*(-uold+unew) every frm_int steps        :767-776
+ *   frames           Uc=U, v=a1*(-uold+unew), a=a0*(uold-2*U+unew)
+ *                    every frm_int steps                          :765-885
  *   blow-up guard    max(UZ)>10*h or isnan(unew(3))               :786-804
  * Expression order inside each formula is the reference's (MATLAB evaluates
  * left to right).  Element work runs in parallel with OpenMP; every basket
@@ -72,9 +73,12 @@ typedef struct {
   const int32_t *sens_ptr, *sens_el;
   double pzt_thickness, g33, e31, e32, h;
   double *voltage; /* [nft * nsens] */
-  /* frames: every frm_int steps store velocity of component frame_dof
-     (1..5) of every node into frames[c*nnode + node] */
-  int32_t frm_int, frame_dof, nframes_max;
+  /* frames (:765-885): every frm_int steps, field_variable frame_kind
+     (0 velocity, 1 displacement, 2 acceleration, 3 all three) of component
+     frame_dof (0 = all five, else 1..5) of every node, stored as
+     frames[(c*nfields + field)*nnode + node]; fields kind-major
+     (displacement, velocity, acceleration), then DOF order */
+  int32_t frm_int, frame_dof, frame_kind, nframes_max;
   double *frames;
   double *t_frames_step; /* nn of each frame (for t_frames) */
   int32_t nthreads;
@@ -257,12 +261,31 @@ int oracle_flat_shell_run(oracle_args *A) {
     }
     /* outputs: displacement before the update (:752-764) */
     for (int k = 0; k < A->nout; ++k) A->displ[(size_t)(nn - 1) * A->nout + k] = U[A->out_dof[k] - 1];
-    /* frames (velocity) and blow-up guard */
+    /* frames and blow-up guard */
     if (A->frm_int > 0 && nn % A->frm_int == 0) {
       if (A->frames && frame_c < A->nframes_max) {
-        double *fr = A->frames + (size_t)frame_c * A->nnode;
-        const int comp = A->frame_dof - 1;
-        for (int q = 0; q < A->nnode; ++q) fr[q] = A->a1 * (-uold[5 * q + comp] + unew[5 * q + comp]);
+        /* API kind -> 0 displacement, 1 velocity, 2 acceleration */
+        static const int kind_slot[3] = {1, 0, 2};
+        const int nkind = A->frame_kind == 3 ? 3 : 1;
+        const int ncomp = A->frame_dof == 0 ? 5 : 1;
+        int fld = 0;
+        for (int k = 0; k < 3; ++k) {
+          if (A->frame_kind != 3 && kind_slot[A->frame_kind] != k) continue;
+          for (int comp = 0; comp < 5; ++comp) {
+            if (A->frame_dof != 0 && A->frame_dof - 1 != comp) continue;
+            double *fr = A->frames + ((size_t)frame_c * nkind * ncomp + fld) * A->nnode;
+            for (int q = 0; q < A->nnode; ++q) {
+              const size_t d = 5 * (size_t)q + comp;
+              if (k == 0)
+                fr[q] = U[d];
+              else if (k == 1)
+                fr[q] = A->a1 * (-uold[d] + unew[d]);
+              else
+                fr[q] = A->a0 * (uold[d] - 2 * U[d] + unew[d]);
+            }
+            ++fld;
+          }
+        }
         if (A->t_frames_step) A->t_frames_step[frame_c] = nn;
         ++frame_c;
       }
