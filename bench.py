@@ -298,6 +298,43 @@ def single_plate_bench(pkg, args):
     print(json.dumps(out))
 
 
+def wavefield_bench(pkg, args):
+    """Wavefield frames -> grid (spec2meshgrid_flat_shell.m) on the config-2
+    plate (200x200 elements, 1.0 M nodes): FP32 forward solve recording all
+    five velocity components every 40 steps, then the 512x512 grid of motion 9
+    (total velocity, top surface, all five fields per node) interpolated from
+    the device-resident frames.  Reports grid points x frames per second of
+    the interpolation kernel (CUDA events) and checks it against the host-frame
+    path."""
+    import torch
+    W = pkg.workloads
+    scs, run = W.plate_pzt(nft=2001)
+    run.frm_int, run.frame_dof, run.frame_kind = 40, 0, 0
+    plan = pkg.Plan(scs, run, precision=32, path=0, steps_per_graph=50)
+    plan.forward(want_frames=False)
+    torch.cuda.synchronize()
+    nfr = plan.info["nframes"]
+    n = 512
+    t0 = time.perf_counter()
+    g = pkg.wavefield.Grid(scs[0].mesh, n, n, "top")
+    setup_s = time.perf_counter() - t0
+    ms = g.time(plan, 9, run.h, "velocity", reps=max(args.steps, 3))
+    img = g.from_plan(plan, 9, run.h, "velocity")
+    host = plan.read_outputs(want_frames=True)[0]["frames"]
+    img_h = g.interpolate(host, [0, 1, 2, 3, 4], 9, run.h)
+    nnode = int(np.asarray(scs[0].mesh["coords"]).shape[0])
+    uniq = nfr * (5 * nnode * 4 + n * n * 8)        # each field value read once, each pixel written once
+    out = {"workload": "wavefield grid 512x512, motion 9, top, config-2 plate", "nnode": nnode, "frames": nfr,
+           "setup_s": setup_s, "max_err_m": g.points()["max_err"], "kernel_ms": ms,
+           "points_frames_per_s": n * n * nfr / (ms / 1e3),
+           "unique_bytes_gbs": uniq / (ms / 1e3) / 1e9,
+           "plan_vs_host_frames_max_abs": float(np.abs(img - img_h).max()),
+           "peak_abs": float(np.abs(img).max())}
+    g.close()
+    plan.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,7 +351,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adjoint", action="store_true", help="damage-gradient workload instead of the forward batch")
-    ap.add_argument("--workload", choices=("batch", "force", "pzt", "solid"), default="batch",
+    ap.add_argument("--workload", choices=("batch", "force", "pzt", "solid", "wavefield"), default="batch",
                     help="batch: 512 plates (default); force: 20x20-element plate; pzt: 200x200 plate with PZT")
     ap.add_argument("--adj-maps", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=20000)
@@ -330,6 +367,8 @@ def main():
         return adjoint_bench(pkg, args)
     if args.plain_fp64:
         return plain_fp64_bench(pkg, args)
+    if args.workload == "wavefield":
+        return wavefield_bench(pkg, args)
     if args.workload != "batch":
         return single_plate_bench(pkg, args)
     W = pkg.workloads

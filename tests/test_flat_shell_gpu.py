@@ -25,7 +25,8 @@ def oracle_run(sc, run, **kw):
     sens = [np.asarray(s) for s in sc.sensors]
     return orc, orc.run(run.dt, run.nft, sc.signal, nn_first=run.nn_first, eta_xy=run.eta_xy, eta_z=run.eta_z,
                         force_dof=sc.force_dof, force_val=sc.force_val, out_dof=sc.out_dof, sensors=sens,
-                        pzt=sc.pzt, h=run.h, frm_int=run.frm_int, frame_dof=run.frame_dof, **kw)
+                        pzt=sc.pzt, h=run.h, frm_int=run.frm_int, frame_dof=run.frame_dof,
+                        frame_kind=run.frame_kind, **kw)
 
 
 def small_case(pkg, nex=5, ney=4, T=4e-5, nft_cap=400, frames=0, sensors=False, keep=False):
