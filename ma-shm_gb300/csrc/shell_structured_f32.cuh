@@ -53,7 +53,6 @@ template <int EW> struct F32Geom {
   static constexpr int UGS = URAW + ((16 - URAW % 32) + 64) % 32;   // group stride = 16 mod 32
   static constexpr int FRAW = 6 * 5 * W;
   static constexpr int FGS = FRAW + ((16 - FRAW % 32) + 64) % 32;
-  static constexpr int NUPD = (G * 6 * OWN + CTA_THREADS - 1) / CTA_THREADS;  // update nodes per thread
 };
 
 template <int EW>
@@ -165,6 +164,9 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   using GM = F32Geom<EW>;
   constexpr int G = GM::G;
   constexpr int W = GM::W;
+  constexpr int OWN = GM::OWN;
+  constexpr int NCOL = (OWN + 31) / 32;  // update passes over a band row's owned columns
+  constexpr int UR = GM::URING;
   extern __shared__ __align__(16) unsigned char smraw[];
   float* sm = reinterpret_cast<float*>(smraw);
   float* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
@@ -188,20 +190,10 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false;
-  // owned band entries this thread updates: (group, logical row, owned column)
-  int ent_g[GM::NUPD], ent_r[GM::NUPD], ent_c[GM::NUPD];
-#pragma unroll
-  for (int s = 0; s < GM::NUPD; ++s) {
-    const int idx = threadIdx.x + s * CTA_THREADS;
-    const bool ok = idx < G * 6 * GM::OWN;
-    ent_g[s] = ok ? idx / (6 * GM::OWN) : 0;
-    const int rem = idx % (6 * GM::OWN);
-    ent_r[s] = rem / GM::OWN;
-    ent_c[s] = ok ? rem % GM::OWN : -1;
-  }
-  float uo_r[GM::NUPD][5];
-  float mt_r[GM::NUPD], mr_r[GM::NUPD];
-  int64_t node_r[GM::NUPD];
+  // update prefetch: warp j finalises logical band row j of every lane group,
+  // owned columns c = lane + 32*s
+  float uo_r[G][NCOL][5];
+  float mt_r[G][NCOL], mr_r[G][NCOL];
 
   __shared__ GroupTask gt[G];  // task facts of the lane groups (shared, not in registers)
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
@@ -211,16 +203,43 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     int maxrows = 0;
 #pragma unroll
     for (int gg = 0; gg < G; ++gg) maxrows = max(maxrows, gt[gg].nrows);
+    // this lane's element column, kept in registers for the whole task
     const GroupTask& t = pick<G>(gt, g);
+    const int t_nrows = t.nrows, t_nex = t.nex;
     const int ex = t.strip * (EW - 1) - 1 + q;
+    const bool colok = ex >= 0 && ex < t_nex;
+    const long long eg0 = t.egrid0 + (long long)t.eyA * t_nex + ex;
+    const float t_sx = t.sx, t_sy = t.sy, t_area4 = t.area4;
     float* ub = ring + g * GM::UGS;
     float* fb = band + g * GM::FGS;
-    const float2 wsxy = make_float2(t.sx, t.sy);
+    const float2 wsxy = make_float2(t_sx, t_sy);
+    // band row j of group gg is final at element rows r in [ulo, uhi), and
+    // for j == 5 only at the plate's last element row; node of column c at
+    // element row r: ub0 + r*ustr + c, valid for c < ucol
+    long long ub0[G];
+    int ustr[G], ulo[G], uhi[G], ucol[G];
+#pragma unroll
+    for (int gg = 0; gg < G; ++gg) {
+      const GroupTask& t2 = pick<G>(gt, gg);
+      const int ix0 = 5 * t2.strip * (EW - 1);
+      ub0[gg] = t2.node0 + (long long)(5 * t2.eyA + j) * t2.NX + ix0;
+      ustr[gg] = 5 * t2.NX;
+      ulo[gg] = t2.block > 0 ? 1 : 0;
+      uhi[gg] = t2.has ? t2.nrows : 0;
+      if (j == 5) {  // the top node row is shared with the next element row
+        const int last = t2.ney - 1 - t2.eyA;
+        ulo[gg] = max(ulo[gg], last);
+        uhi[gg] = min(uhi[gg], last + 1);
+      }
+      ucol[gg] = min(OWN, t2.NX - ix0);
+    }
 
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
     ring_load<EW>(ring, cur, a.nnode_pad, gt, 0, 6);
     cp_async_commit();
 
+    int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
+    int rb6 = 0;  // r mod 6
     for (int r = 0; r < maxrows; ++r) {
       // next element row's five new node rows (ring slots free since row r-1)
       if (r + 1 < maxrows) ring_load<EW>(ring, cur, a.nnode_pad, gt, 5 * r + 6, 5);
@@ -228,15 +247,14 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       __syncthreads();
 
-      const int ey = t.eyA + r;
-      const bool rowact = r < t.nrows;
-      const bool valid = rowact && ex >= 0 && ex < t.nex;
-      const int64_t egrid = t.egrid0 + (int64_t)ey * t.nex + ex;
-      const int s0 = 5 * r;  // first node row of this element row (task-relative)
+      const bool rowact = r < t_nrows;
+      const bool valid = rowact && colok;
+      const long long egrid = eg0 + (long long)r * t_nex;
+      auto slot = [rb](int k) { const int s = rb + k; return s >= UR ? s - UR : s; };
 
       // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
       if (valid) {
-        const float* urow = ub + ((s0 + j) % GM::URING) * 5 * W + 5 * q;
+        const float* urow = ub + slot(j) * 5 * W + 5 * q;
         float2 acc[5][3];
 #pragma unroll
         for (int f = 0; f < 5; ++f)
@@ -250,7 +268,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
             for (int p = 0; p < 3; ++p) acc[f][p] = fma2(c_Dp[k][p], u2, acc[f][p]);
           }
-        const float2 sx2 = bc2(t.sx);
+        const float2 sx2 = bc2(t_sx);
 #pragma unroll
         for (int f = 0; f < 5; ++f)
 #pragma unroll
@@ -267,7 +285,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         float v[5][NP];
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
-          const float* urow = ub + ((s0 + k) % GM::URING) * 5 * W + 5 * q + i;
+          const float* urow = ub + slot(k) * 5 * W + 5 * q + i;
 #pragma unroll
           for (int f = 0; f < 5; ++f) v[f][k] = urow[f * W];
         }
@@ -284,7 +302,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             for (int p = 0; p < 3; ++p) de2[f][p] = fma2(c_Dp[m][p], v2, de2[f][p]);
           }
 #pragma unroll
-          for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t.sy));
+          for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
         }
         float2 L[LAMP];
         {
@@ -331,7 +349,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           MM = fma2(L[17], bc2(kxy), MM);         // (Myy, Mxy)
           float2 QQ = mul2(L[18], bc2(gyz));
           QQ = fma2(L[19], bc2(gxz), QQ);         // (Qy, Qx)
-          const float Wn = c_w32[i] * c_w32[k] * t.area4;
+          const float Wn = c_w32[i] * c_w32[k] * t_area4;
           const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
           // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
           const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
@@ -369,24 +387,24 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       __syncthreads();
 
-      // the update's global loads for this element row, issued before phase C
+      // the update's global loads for band row j, issued before phase C
+      bool rowok[G];
+      long long rowbase[G];
 #pragma unroll
-      for (int s = 0; s < GM::NUPD; ++s) {
-        node_r[s] = -1;
-        if (ent_c[s] < 0) continue;
-        const GroupTask& t2 = pick<G>(gt, ent_g[s]);
-        const int rr = ent_r[s];
-        if (!t2.has || r >= t2.nrows || (t2.block > 0 && r == 0)) continue;
-        const int ey2 = t2.eyA + r;
-        if (rr >= ((ey2 == t2.ney - 1) ? 6 : 5)) continue;
-        const int ix = 5 * t2.strip * (EW - 1) + ent_c[s];
-        if (ix >= t2.NX) continue;
-        const int64_t node = t2.node0 + (int64_t)(5 * ey2 + rr) * t2.NX + ix;
-        node_r[s] = node;
-        mt_r[s] = a.minv[node];
-        mr_r[s] = a.minv[a.nnode_pad + node];
+      for (int gg = 0; gg < G; ++gg) {
+        rowok[gg] = r >= ulo[gg] && r < uhi[gg];
+        rowbase[gg] = ub0[gg] + (long long)r * ustr[gg];
 #pragma unroll
-        for (int f = 0; f < 5; ++f) uo_r[s][f] = prev[f * a.nnode_pad + node];
+        for (int s = 0; s < NCOL; ++s) {
+          const int c = lane + 32 * s;
+          if (rowok[gg] && c < ucol[gg]) {
+            const long long node = rowbase[gg] + c;
+            mt_r[gg][s] = a.minv[node];
+            mr_r[gg][s] = a.minv[a.nnode_pad + node];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) uo_r[gg][s][f] = prev[f * a.nnode_pad + node];
+          }
+        }
       }
 
       // phase C: xi-part of the transposed operator + column part
@@ -420,8 +438,10 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       // is added to; rows 1..5 start here, so pass 1 stores columns i = 0..4
       // (lanes without an element store zeros) and pass 2 adds column i = 5
       // (the next lane's column 0), or stores it on the strip's last lane.
+      int prow = j - rb6;
+      if (prow < 0) prow += 6;
       {
-        float* dst = fb + ((j - r % 6 + 6) % 6) * 5 * W + 5 * q;
+        float* dst = fb + prow * 5 * W + 5 * q;
         if (j == 0) {
 #pragma unroll
           for (int f = 0; f < 5; ++f)
@@ -445,51 +465,57 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
       if (kSensor && j == 0 && valid && owned_row && q > 0) {
-        const int slot = a.esens_g[egrid];
-        if (slot >= 0) {
-          double s = 0.0;
+        const int sl = a.esens_g[egrid];
+        if (sl >= 0) {
+          double sum = 0.0;
 #pragma unroll
-          for (int i = 0; i < NP; ++i) s += (double)vred[i * CTA_ELEMS + lane];
-          a.vsum[(int64_t)slot * a.nft + (nn - 1)] = s;
+          for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
+          a.vsum[(int64_t)sl * a.nft + (nn - 1)] = sum;
         }
       }
-      // update owned, complete nodes (excitation added here by the node's owner)
+      // update owned, complete nodes of band row j (excitation added here by
+      // the node's owner)
 #pragma unroll
-      for (int s = 0; s < GM::NUPD; ++s) {
-        if (node_r[s] < 0) continue;
-        const int gg = ent_g[s], rr = ent_r[s], c = ent_c[s];
-        const GroupTask& t2 = pick<G>(gt, gg);
-        const float* bnd = band + gg * GM::FGS + ((rr - r % 6 + 6) % 6) * 5 * W + 5 + c;
-        const float* urow = ring + gg * GM::UGS + ((5 * r + rr) % GM::URING) * 5 * W + 5 + c;
-        const int64_t node = node_r[s];
-        float F[5];
+      for (int gg = 0; gg < G; ++gg)
 #pragma unroll
-        for (int f = 0; f < 5; ++f) F[f] = bnd[f * W];
-        if (t2.fn > 0) {
-          const int iy = 5 * (t2.eyA + r) + rr;
-          for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)
-            if (a.f_iy[fi] == iy && a.f_xl[fi] == 5 + c) {
-              const float fs = (float)(a.f_val[fi] * a.st[(int64_t)t2.scen * a.nft + (nn - 1)]);
+        for (int s = 0; s < NCOL; ++s) {
+          const int c = lane + 32 * s;
+          if (!(rowok[gg] && c < ucol[gg])) continue;
+          const float* bnd = band + gg * GM::FGS + prow * 5 * W + 5 + c;
+          const float* urow = ring + gg * GM::UGS + slot(j) * 5 * W + 5 + c;
+          const long long node = rowbase[gg] + c;
+          float F[5];
 #pragma unroll
-              for (int f = 0; f < 5; ++f)
-                if (f == a.f_field[fi]) F[f] -= fs;
+          for (int f = 0; f < 5; ++f) F[f] = bnd[f * W];
+          const GroupTask& t2 = pick<G>(gt, gg);
+          if (t2.fn > 0) {
+            const int iy = 5 * (t2.eyA + r) + j;
+            for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)
+              if (a.f_iy[fi] == iy && a.f_xl[fi] == 5 + c) {
+                const float fs = (float)(a.f_val[fi] * a.st[(int64_t)t2.scen * a.nft + (nn - 1)]);
+#pragma unroll
+                for (int f = 0; f < 5; ++f)
+                  if (f == a.f_field[fi]) F[f] -= fs;
+              }
+          }
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            const float u = urow[f * W];
+            const float uo = uo_r[gg][s][f];
+            const float im = (f == 1 || f == 3) ? mr_r[gg][s] : mt_r[gg][s];
+            const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
+            prev[f * a.nnode_pad + node] = un;
+            if (frame) {
+              store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
+              if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
             }
-        }
-#pragma unroll
-        for (int f = 0; f < 5; ++f) {
-          const float u = urow[f * W];
-          const float uo = uo_r[s][f];
-          const float im = (f == 1 || f == 3) ? mr_r[s] : mt_r[s];
-          const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
-          prev[f * a.nnode_pad + node] = un;
-          if (frame) {
-            store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
-            if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
           }
         }
-      }
       // ring slots read above are refilled by the next row's prefetch
       __syncthreads();
+      rb += 5;
+      if (rb >= UR) rb -= UR;
+      if (++rb6 == 6) rb6 = 0;
     }
     cp_async_wait_all();
     __syncthreads();
