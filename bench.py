@@ -177,7 +177,7 @@ def adjoint_bench(pkg, args):
     ndof = W.dof_count(scs)
     out = {"metric": "adjoint gradient cost / forward cost", "maps": len(scs), "dof": ndof, "nft": run.nft,
            "ckpt_every": 200, "dtype": "f32 stepping, f64 misfit and gradient"}
-    times = {}
+    times, t_adj, grads = {}, {}, {}
     for path in (1, 2):
         p = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=50)
         p.forward()
@@ -186,17 +186,21 @@ def adjoint_bench(pkg, args):
         p.forward()
         torch.cuda.synchronize()
         times[path] = time.perf_counter() - t0
-        if path == 1:
-            t0 = time.perf_counter()
-            mis32, g32 = p.forward_backward(targets, ckpt_every=200)
-            torch.cuda.synchronize()
-            t_adj = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        mis32, grads[path] = p.forward_backward(targets, ckpt_every=200)
+        torch.cuda.synchronize()
+        t_adj[path] = time.perf_counter() - t0
+        out[f"phases_ms_path{path}"] = p.forward_backward_timing()
         p.close()
+    g32 = grads[2]
     out["forward_s_general_path"] = times[1]
     out["forward_s_structured_path"] = times[2]
-    out["forward_backward_s"] = t_adj
-    out["ratio_vs_forward_same_path"] = t_adj / times[1]
-    out["ratio_vs_fastest_forward"] = t_adj / min(times.values())
+    out["forward_backward_s_general_path"] = t_adj[1]
+    out["forward_backward_s_structured_path"] = t_adj[2]
+    out["ratio_vs_forward_same_path"] = {str(k): t_adj[k] / times[k] for k in (1, 2)}
+    out["ratio_vs_fastest_forward"] = min(t_adj.values()) / min(times.values())
+    out["grad_rel_diff_structured_vs_general_fp32"] = max(
+        float(np.linalg.norm(grads[2][i] - grads[1][i]) / np.linalg.norm(grads[1][i])) for i in range(len(scs)))
     # FP64 reference gradient on the first maps
     nref = min(4, len(scs))
     p = pkg.Plan(scs[:nref], run, precision=64, path=1)

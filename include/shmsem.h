@@ -184,6 +184,9 @@ shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh *meshes, co
  *   target [nscen][nft x n_out] column-major per scenario, like displ. */
 shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *target, double *misfit,
                                 double *grad, int32_t ckpt_every, void *stream);
+/* Device time (ms, CUDA events) of the last shm_forward_backward's phases:
+ * [0] forward pass with checkpoints, [1] segment recomputes, [2] adjoint steps. */
+shm_status shm_forward_backward_timing(const shm_plan *plan, float *ms3);
 
 /* Autotuner for plans on the structured path: times `steps` steps of the
  * general kernels and of every (elements per lane group, element rows per

@@ -39,6 +39,7 @@ template <typename T> struct StructArgs {
   int64_t nnode_pad;
   T* UA;
   T* UB;
+  T* outp;  // u_{n+1} destination; null = over u_{n-1}
   const T* __restrict__ minv;
   T k1[5], k2[5];
   const T* __restrict__ mat;
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
           const T uo = prev[f * a.nnode_pad + node];
           const T im = (f == 1 || f == 3) ? mr : mt;
           const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F);
-          prev[f * a.nnode_pad + node] = un;
+          (a.outp ? a.outp : prev)[f * a.nnode_pad + node] = un;
           if (frame) {
             store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
             if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;

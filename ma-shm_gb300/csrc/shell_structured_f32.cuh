@@ -68,6 +68,7 @@ struct F32Args {
   int64_t nnode_pad;
   float* UA;
   float* UB;
+  float* outp;  // u_{n+1} destination; null = over u_{n-1}
   const float* __restrict__ minv;
   float k1[5], k2[5];
   const float2* __restrict__ matp;  // [nmat][20] coefficient pairs
@@ -177,6 +178,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   const bool odd = ((nn - a.nn_first) & 1);
   const float* __restrict__ cur = odd ? a.UB : a.UA;
   float* prev = odd ? a.UA : a.UB;
+  float* dst = a.outp ? a.outp : prev;
   if (blockIdx.x == 0)
     for (int q = threadIdx.x; q < a.nout; q += blockDim.x)
       a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             const float uo = uo_r[gg][s][f];
             const float im = (f == 1 || f == 3) ? mr_r[gg][s] : mt_r[gg][s];
             const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
-            prev[f * a.nnode_pad + node] = un;
+            dst[f * a.nnode_pad + node] = un;
             if (frame) {
               store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
               if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;

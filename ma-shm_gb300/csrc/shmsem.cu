@@ -38,6 +38,7 @@ template <typename T> struct GenArgs {
   // state (two SoA buffers [5][nnode_pad]) and scratch [5][plane]
   T* UA;
   T* UB;
+  T* outp;                        // u_{n+1} destination; null = over u_{n-1} (ping-pong)
   T* F2;
   // mesh
   const int* __restrict__ conn;   // [36][fen_pad], 0-based global nodes
@@ -74,8 +75,7 @@ template <typename T> struct GenArgs {
   // adjoint (k_elem_adjoint only)
   int nadj;                       // adjoint force slots, one per point output
   const double* __restrict__ asig;  // [nout][nft] misfit residuals in reversed time
-  const T* __restrict__ seg;      // forward states of the current segment [k][5][nnode_pad]
-  int seg_base;                   // segment slice = seg_base - nn
+  const T* __restrict__ um;       // forward state u_{n-1} paired with this adjoint step
   double* grad;                   // [fen_pad] dJ/dd_e accumulated in FP64
 };
 
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(CTA_THREADS) k_elem_adjoint(GenArgs<T> a, int 
   T out[5][NP];
   row_transpose_apply(xs, ys, j, out);
   // gradient partial: (K_e^0 lambda)' u_{n-1} over the row's nodes
-  const T* __restrict__ um = a.seg + (int64_t)(a.seg_base - nn) * 5 * a.nnode_pad;
+  const T* __restrict__ um = a.um;
   double dot = 0.0;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
 #pragma unroll
     for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
   }
+  T* dst = a.outp ? a.outp : prev;
   const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   bool bad = false;
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
     // unew = mg0.*(-F + mg2.*U - mg.*uold + a1*cg.*uold) rewritten as
     // u + k1*(u-uold) - k2*(F/M); F already contains -Fa*st(nn)
     const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
-    prev[f * a.nnode_pad + g] = un;
+    dst[f * a.nnode_pad + g] = un;
     if (frame) {
       store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
       if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
@@ -379,6 +380,9 @@ struct shm_plan {
   bool sp_generic = false;  // FP32 structured: use the generic template instead of the packed kernel
   // adjoint buffers (allocated by the first shm_forward_backward)
   void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr;
+  // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
+  void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
+  float fb_ms[3] = {0.f, 0.f, 0.f};  // last forward_backward: forward, recompute, adjoint (ms)
   double *grad = nullptr, *asig = nullptr;
   int* d_base_adj = nullptr;
   int seg_k = 0, nck = 0;
@@ -588,8 +592,9 @@ template <typename T> static GenArgs<T> make_args(shm_plan* p) {
   a.fen = (int)p->fen;
   a.nn_first = p->nn_first;
   a.nft = p->nft;
-  a.UA = (T*)p->UA;
-  a.UB = (T*)p->UB;
+  a.UA = (T*)(p->ov_UA ? p->ov_UA : p->UA);
+  a.UB = (T*)(p->ov_UB ? p->ov_UB : p->UB);
+  a.outp = (T*)p->ov_out;
   a.F2 = (T*)p->F2;
   a.conn = p->conn;
   a.geo = (const T*)p->geo;
@@ -904,8 +909,9 @@ static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s
   a.nn_first = p->nn_first;
   a.nft = p->nft;
   a.nnode_pad = p->nnode_pad;
-  a.UA = (float*)p->UA;
-  a.UB = (float*)p->UB;
+  a.UA = (float*)(p->ov_UA ? p->ov_UA : p->UA);
+  a.UB = (float*)(p->ov_UB ? p->ov_UB : p->UB);
+  a.outp = (float*)p->ov_out;
   a.minv = (const float*)p->minv;
   for (int f = 0; f < 5; ++f) {
     a.k1[f] = (float)p->k1[f];
@@ -960,8 +966,9 @@ static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.nn_first = p->nn_first;
   a.nft = p->nft;
   a.nnode_pad = p->nnode_pad;
-  a.UA = (T*)p->UA;
-  a.UB = (T*)p->UB;
+  a.UA = (T*)(p->ov_UA ? p->ov_UA : p->UA);
+  a.UB = (T*)(p->ov_UB ? p->ov_UB : p->UB);
+  a.outp = (T*)p->ov_out;
   a.minv = (const T*)p->minv;
   for (int f = 0; f < 5; ++f) {
     a.k1[f] = (T)p->k1[f];
@@ -1734,9 +1741,9 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     p->LA = la;
     p->LB = lb;
   }
-  if (p->seg_k < k) {
+  if (p->seg_k < k) {  // slots 1..k of a segment's recomputed states (slot 0 = the checkpoint)
     T* sg = nullptr;
-    if ((st_ = dalloc(p, &sg, (size_t)k * S)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &sg, (size_t)(k + 1) * S)) != SHM_OK) return st_;
     p->seg = sg;
     p->seg_k = k;
   }
@@ -1751,22 +1758,28 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   T* ck = (T*)p->ck;
   T* seg = (T*)p->seg;
   const size_t SB = S * sizeof(T);
-  // 1. forward pass, checkpoint (u_n, u_{n-1}) every k steps
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
+  float t_rec = 0.f, t_adj = 0.f;
+  // 1. forward pass with the plan's own step kernels (the structured fused
+  // kernel when the plan uses it), checkpoint (u_n, u_{n-1}) every k steps
   if ((st_ = shm_reset(p)) != SHM_OK) return st_;
   if ((st_ = shm_set_signal(p, st, s)) != SHM_OK) return st_;
+  cudaEventRecord(ev[0], s);
   for (int j = 0; j < nck; ++j) {
     const int n = n0 + j * k;
     const bool odd = ((n - n0) & 1);
     CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S, odd ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
     CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S + S, odd ? UA : UB, SB, cudaMemcpyDeviceToDevice, s));
-    const int cnt = std::min(k, N - n + 1);
-    for (int kk = 0; kk < cnt; ++kk) CKP(p, launch_general_step<T>(p, kk, s));
-    k_advance<<<1, 1, 0, s>>>(p->d_base, cnt);
+    if ((st_ = advance_async(p, std::min(k, N - n + 1), s)) != SHM_OK) return st_;
   }
+  cudaEventRecord(ev[1], s);
   // 2. misfit (FP64) and the residuals in reversed time
   std::vector<double> disp((size_t)std::max(p->nout, 1) * N);
   CKP(p, cudaMemcpyAsync(disp.data(), p->displ, sizeof(double) * disp.size(), cudaMemcpyDeviceToHost, s));
   CKP(p, cudaStreamSynchronize(s));
+  float t_fwd = 0.f;
+  cudaEventElapsedTime(&t_fwd, ev[0], ev[1]);
   std::vector<double> asig((size_t)std::max(p->nout, 1) * N, 0.0);
   for (int sc = 0; sc < p->nscen; ++sc) {
     double J = 0.0;
@@ -1779,7 +1792,9 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     if (misfit) misfit[sc] = J;
   }
   CKP(p, cudaMemcpyAsync(p->asig, asig.data(), sizeof(double) * asig.size(), cudaMemcpyHostToDevice, s));
-  // 3. backward: recompute each segment forward, then step the adjoint back through it
+  // 3. backward: recompute each segment forward into its state slots with the
+  // forward pass's step kernels (bit-identical states, no copies), then step
+  // the adjoint back through it
   CKP(p, cudaMemsetAsync(p->LA, 0, SB, s));
   CKP(p, cudaMemsetAsync(p->LB, 0, SB, s));
   CKP(p, cudaMemsetAsync(p->grad, 0, sizeof(double) * p->fen_pad, s));
@@ -1787,42 +1802,63 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   GenArgs<T> a = make_args<T>(p);
   a.UA = (T*)p->LA;
   a.UB = (T*)p->LB;
+  a.outp = nullptr;
   a.d_base = p->d_base_adj;
   a.nadj = p->nout;
   a.asig = p->asig;
-  a.seg = seg;
   a.grad = p->grad;
   a.fs.frm_int = 0;
   a.nout = 0;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
   std::vector<int> hbase(1);
+  int nn_adj = n0;  // adjoint loop index of the segment's first adjoint step
   for (int j = nck - 1; j >= 0; --j) {
     const int sj = n0 + j * k, ej = std::min(sj + k - 1, N);
-    const bool odd = ((sj - n0) & 1);
-    CKP(p, cudaMemcpyAsync(odd ? UB : UA, ck + (size_t)j * 2 * S, SB, cudaMemcpyDeviceToDevice, s));
-    CKP(p, cudaMemcpyAsync(odd ? UA : UB, ck + (size_t)j * 2 * S + S, SB, cudaMemcpyDeviceToDevice, s));
+    const int cnt = ej - sj + 1;
+    T* ck_u = ck + (size_t)j * 2 * S;
+    T* ck_uo = ck_u + S;
+    auto state = [&](int i) -> T* { return i < 0 ? ck_uo : (i == 0 ? ck_u : seg + (size_t)i * S); };
     hbase[0] = sj;
+    cudaEventRecord(ev[2], s);
     CKP(p, cudaMemcpyAsync(p->d_base, hbase.data(), 4, cudaMemcpyHostToDevice, s));
     // the forward recompute must not see the adjoint residual forces
     for (int f = 0; f < 5; ++f)
       CKP(p, cudaMemsetAsync((T*)p->F2 + f * p->plane + (int64_t)NPE * p->fen_pad + p->nforce, 0,
                              sizeof(T) * p->nout, s));
-    for (int n = sj; n <= ej; ++n) {
-      const bool o2 = ((n - n0) & 1);
-      CKP(p, cudaMemcpyAsync(seg + (size_t)(n - sj) * S, o2 ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
-      if (n < ej) CKP(p, launch_general_step<T>(p, n - sj, s));
+    for (int i = 0; i + 1 < cnt; ++i) {
+      const bool odd = ((sj + i - n0) & 1);
+      p->ov_UA = odd ? state(i - 1) : state(i);
+      p->ov_UB = odd ? state(i) : state(i - 1);
+      p->ov_out = state(i + 1);
+      cudaError_t e = launch_step(p, i, s);
+      p->ov_UA = p->ov_UB = p->ov_out = nullptr;
+      if (e != cudaSuccess) {
+        p->err = std::string("recompute: ") + cudaGetErrorString(e);
+        return SHM_ERR_CUDA;
+      }
     }
-    a.seg_base = N + n0 - sj;
-    const int cnt = ej - sj + 1;
+    cudaEventRecord(ev[3], s);
     for (int kk = 0; kk < cnt; ++kk) {
+      a.um = state(N + n0 - (nn_adj + kk) - sj);  // u at forward time N + n0 - nn
       k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, s>>>(a, kk);
       k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kk);
     }
     k_advance<<<1, 1, 0, s>>>(p->d_base_adj, cnt);
+    nn_adj += cnt;
     CKP(p, cudaGetLastError());
+    cudaEventRecord(ev[0], s);
     CKP(p, cudaStreamSynchronize(s));  // hbase is reused by the next segment
+    float t1 = 0.f, t2 = 0.f;
+    cudaEventElapsedTime(&t1, ev[2], ev[3]);
+    cudaEventElapsedTime(&t2, ev[3], ev[0]);
+    t_rec += t1;
+    t_adj += t2;
   }
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  p->fb_ms[0] = t_fwd;
+  p->fb_ms[1] = t_rec;
+  p->fb_ms[2] = t_adj;
   std::vector<double> g((size_t)p->fen_pad);
   CKP(p, cudaMemcpyAsync(g.data(), p->grad, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
   // leave the adjoint slots zero for later forward runs
@@ -1835,6 +1871,12 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   shm_status div = check_flag(p, s);
   st_ = shm_reset(p);
   return div != SHM_OK ? div : st_;
+}
+
+extern "C" shm_status shm_forward_backward_timing(const shm_plan* p, float* ms3) {
+  if (!p || !ms3) return SHM_ERR_BAD_ARG;
+  for (int i = 0; i < 3; ++i) ms3[i] = p->fb_ms[i];
+  return SHM_OK;
 }
 
 extern "C" shm_status shm_forward_backward(shm_plan* p, const double* st, const double* target, double* misfit,

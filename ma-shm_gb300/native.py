@@ -85,6 +85,7 @@ SIGNATURES = {
     "shm_solid_plan_create": (C.c_int, [C.c_int32, C.POINTER(ShmSolidMesh), C.POINTER(ShmSolidMaterial),
                                         C.POINTER(ShmRun), C.POINTER(ShmOptions), C.POINTER(C.c_void_p)]),
     "shm_forward_backward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_int32, C.c_void_p]),
+    "shm_forward_backward_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "shm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_float)]),
     "shm_stiffness_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

@@ -111,6 +111,13 @@ class Plan:
             e0 += fen
         return mis, out
 
+    def forward_backward_timing(self) -> dict:
+        """Device ms of the last forward_backward's forward pass, segment
+        recomputes and adjoint steps."""
+        ms = (C.c_float * 3)()
+        self._check(self.lib.shm_forward_backward_timing(self.handle, ms))
+        return dict(forward_ms=ms[0], recompute_ms=ms[1], adjoint_ms=ms[2])
+
     def _arr(self, a, dtype):
         a = np.ascontiguousarray(a, dtype=dtype)
         self._keep.append(a)

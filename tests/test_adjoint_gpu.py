@@ -112,3 +112,22 @@ def test_adjoint_batch_equals_solo(pkg):
         p1.close()
         np.testing.assert_array_equal(grads[s], g1[0])
         assert mis[s] == m1[0]
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_adjoint_on_structured_plan(pkg, prec):
+    """A plan on the structured fused kernels runs its forward pass and the
+    segment recomputes on those kernels (recompute bit-identical to the
+    forward pass); the gradient matches the general-path plan's."""
+    sc, run, target = adjoint_case(pkg, seed=4)
+    res = {}
+    for path in (1, 2):
+        plan = pkg.Plan([sc], run, precision=prec, path=path)
+        assert plan.info["path"] == path
+        res[path] = plan.forward_backward([target], ckpt_every=37)
+        t = plan.forward_backward_timing()
+        assert t["forward_ms"] > 0 and t["recompute_ms"] > 0 and t["adjoint_ms"] > 0
+        plan.close()
+    tol = 1e-10 if prec == 64 else 1e-4
+    assert rel(res[2][1][0], res[1][1][0]) <= tol
+    assert abs(res[2][0][0] - res[1][0][0]) <= tol * res[1][0][0]
