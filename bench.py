@@ -180,6 +180,8 @@ def adjoint_bench(pkg, args):
     times, t_adj, grads = {}, {}, {}
     for path in (1, 2):
         p = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=50)
+        if path == 2:
+            out["autotune_path2"] = p.autotune(10)
         p.forward()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

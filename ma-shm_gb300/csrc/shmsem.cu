@@ -219,14 +219,17 @@ __global__ void __launch_bounds__(CTA_THREADS) k_elem_adjoint(GenArgs<T> a, int 
   T out[5][NP];
   row_transpose_apply(xs, ys, j, out);
   // gradient partial: (K_e^0 lambda)' u_{n-1} over the row's nodes
+  // (one element line's 30 products in the state precision; the per-element
+  // and the across-step sums are FP64)
   const T* __restrict__ um = a.um;
-  double dot = 0.0;
+  T dotl = T(0);
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
     const int node = a.conn[(int64_t)(j * NP + i) * a.fen_pad + e];
 #pragma unroll
-    for (int f = 0; f < 5; ++f) dot += (double)out[f][i] * (double)um[f * a.nnode_pad + node];
+    for (int f = 0; f < 5; ++f) dotl += out[f][i] * um[f * a.nnode_pad + node];
   }
+  const double dot = (double)dotl;
   const T keep = a.ekeep[e];
 #pragma unroll
   for (int f = 0; f < 5; ++f)
@@ -297,6 +300,10 @@ __global__ void k_assemble_only(GenArgs<T> a, T* out) {
 
 __global__ void k_advance(int* d_base, int n) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *d_base += n;
+}
+
+__global__ void k_set(int* d_base, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *d_base = v;
 }
 
 // voltage(nn,k) = mean over the sensor's local nodes (FP64)
@@ -379,7 +386,8 @@ struct shm_plan {
   StructPlan sp;
   bool sp_generic = false;  // FP32 structured: use the generic template instead of the packed kernel
   // adjoint buffers (allocated by the first shm_forward_backward)
-  void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr;
+  void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr, *F2adj = nullptr;
+  cudaStream_t aux[2] = {nullptr, nullptr};  // adjoint: recompute and adjoint streams
   // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
   float fb_ms[3] = {0.f, 0.f, 0.f};  // last forward_backward: forward, recompute, adjoint (ms)
@@ -1369,6 +1377,8 @@ extern "C" shm_status shm_plan_destroy(shm_plan* p) {
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   for (void* q : p->allocs) cudaFree(q);
   if (p->stream) cudaStreamDestroy(p->stream);
+  for (cudaStream_t a : p->aux)
+    if (a) cudaStreamDestroy(a);
   delete p;
   return SHM_OK;
 }
@@ -1741,9 +1751,9 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     p->LA = la;
     p->LB = lb;
   }
-  if (p->seg_k < k) {  // slots 1..k of a segment's recomputed states (slot 0 = the checkpoint)
+  if (p->seg_k < k) {  // two sets of slots 1..k of a segment's recomputed states (slot 0 = the checkpoint)
     T* sg = nullptr;
-    if ((st_ = dalloc(p, &sg, (size_t)(k + 1) * S)) != SHM_OK) return st_;
+    if ((st_ = dalloc(p, &sg, (size_t)2 * (k + 1) * S)) != SHM_OK) return st_;
     p->seg = sg;
     p->seg_k = k;
   }
@@ -1794,15 +1804,40 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   CKP(p, cudaMemcpyAsync(p->asig, asig.data(), sizeof(double) * asig.size(), cudaMemcpyHostToDevice, s));
   // 3. backward: recompute each segment forward into its state slots with the
   // forward pass's step kernels (bit-identical states, no copies), then step
-  // the adjoint back through it
+  // the adjoint back through it.  Segment j-1 is recomputed on one stream
+  // while the adjoint steps through segment j on another (two slot sets, a
+  // separate element-force scratch for the adjoint); both sweeps are
+  // latency-bound, so running them side by side raises the device's use.
+  if (!p->F2adj) {
+    T* f2a = nullptr;
+    if ((st_ = dalloc(p, &f2a, (size_t)5 * p->plane)) != SHM_OK) return st_;
+    p->F2adj = f2a;
+  }
+  for (int i = 0; i < 2; ++i)
+    if (!p->aux[i]) CKP(p, cudaStreamCreateWithFlags(&p->aux[i], cudaStreamNonBlocking));
+  cudaStream_t sr = p->aux[0], sa = p->aux[1];
   CKP(p, cudaMemsetAsync(p->LA, 0, SB, s));
   CKP(p, cudaMemsetAsync(p->LB, 0, SB, s));
+  CKP(p, cudaMemsetAsync(p->F2adj, 0, sizeof(T) * 5 * p->plane, s));
   CKP(p, cudaMemsetAsync(p->grad, 0, sizeof(double) * p->fen_pad, s));
   CKP(p, cudaMemcpyAsync(p->d_base_adj, &n0, 4, cudaMemcpyHostToDevice, s));
+  cudaEvent_t ev_s, ev_end_r, ev_end_a;
+  std::vector<cudaEvent_t> evR(nck), evA(nck);
+  cudaEventCreateWithFlags(&ev_s, cudaEventDisableTiming);
+  cudaEventCreate(&ev_end_r);
+  cudaEventCreate(&ev_end_a);
+  for (int j = 0; j < nck; ++j) {
+    cudaEventCreateWithFlags(&evR[j], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&evA[j], cudaEventDisableTiming);
+  }
+  CKP(p, cudaEventRecord(ev_s, s));
+  CKP(p, cudaStreamWaitEvent(sr, ev_s, 0));
+  CKP(p, cudaStreamWaitEvent(sa, ev_s, 0));
   GenArgs<T> a = make_args<T>(p);
   a.UA = (T*)p->LA;
   a.UB = (T*)p->LB;
   a.outp = nullptr;
+  a.F2 = (T*)p->F2adj;
   a.d_base = p->d_base_adj;
   a.nadj = p->nout;
   a.asig = p->asig;
@@ -1811,49 +1846,66 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   a.nout = 0;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
-  std::vector<int> hbase(1);
-  int nn_adj = n0;  // adjoint loop index of the segment's first adjoint step
-  for (int j = nck - 1; j >= 0; --j) {
-    const int sj = n0 + j * k, ej = std::min(sj + k - 1, N);
-    const int cnt = ej - sj + 1;
+  auto seg_state = [&](int j, int i) -> T* {  // u at forward time sj + i of segment j
     T* ck_u = ck + (size_t)j * 2 * S;
-    T* ck_uo = ck_u + S;
-    auto state = [&](int i) -> T* { return i < 0 ? ck_uo : (i == 0 ? ck_u : seg + (size_t)i * S); };
-    hbase[0] = sj;
-    cudaEventRecord(ev[2], s);
-    CKP(p, cudaMemcpyAsync(p->d_base, hbase.data(), 4, cudaMemcpyHostToDevice, s));
-    // the forward recompute must not see the adjoint residual forces
-    for (int f = 0; f < 5; ++f)
-      CKP(p, cudaMemsetAsync((T*)p->F2 + f * p->plane + (int64_t)NPE * p->fen_pad + p->nforce, 0,
-                             sizeof(T) * p->nout, s));
+    if (i < 0) return ck_u + S;
+    if (i == 0) return ck_u;
+    return seg + ((size_t)(j & 1) * (k + 1) + i) * S;
+  };
+  cudaEventRecord(ev[2], sr);
+  auto recompute = [&](int j) -> shm_status {
+    const int sj = n0 + j * k, cnt = std::min(sj + k - 1, N) - sj + 1;
+    k_set<<<1, 1, 0, sr>>>(p->d_base, sj);
     for (int i = 0; i + 1 < cnt; ++i) {
       const bool odd = ((sj + i - n0) & 1);
-      p->ov_UA = odd ? state(i - 1) : state(i);
-      p->ov_UB = odd ? state(i) : state(i - 1);
-      p->ov_out = state(i + 1);
-      cudaError_t e = launch_step(p, i, s);
+      p->ov_UA = odd ? seg_state(j, i - 1) : seg_state(j, i);
+      p->ov_UB = odd ? seg_state(j, i) : seg_state(j, i - 1);
+      p->ov_out = seg_state(j, i + 1);
+      cudaError_t e = launch_step(p, i, sr);
       p->ov_UA = p->ov_UB = p->ov_out = nullptr;
       if (e != cudaSuccess) {
         p->err = std::string("recompute: ") + cudaGetErrorString(e);
         return SHM_ERR_CUDA;
       }
     }
-    cudaEventRecord(ev[3], s);
+    CKP(p, cudaEventRecord(evR[j], sr));
+    return SHM_OK;
+  };
+  if ((st_ = recompute(nck - 1)) != SHM_OK) return st_;
+  cudaEventRecord(ev[3], sa);
+  int nn_adj = n0;  // adjoint loop index of the segment's first adjoint step
+  for (int j = nck - 1; j >= 0; --j) {
+    const int sj = n0 + j * k, cnt = std::min(sj + k - 1, N) - sj + 1;
+    // adjoint through segment j once its states exist
+    CKP(p, cudaStreamWaitEvent(sa, evR[j], 0));
     for (int kk = 0; kk < cnt; ++kk) {
-      a.um = state(N + n0 - (nn_adj + kk) - sj);  // u at forward time N + n0 - nn
-      k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, s>>>(a, kk);
-      k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kk);
+      a.um = seg_state(j, N + n0 - (nn_adj + kk) - sj);  // u at forward time N + n0 - nn
+      k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, sa>>>(a, kk);
+      k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, sa>>>(a, kk);
     }
-    k_advance<<<1, 1, 0, s>>>(p->d_base_adj, cnt);
-    nn_adj += cnt;
+    k_advance<<<1, 1, 0, sa>>>(p->d_base_adj, cnt);
     CKP(p, cudaGetLastError());
-    cudaEventRecord(ev[0], s);
-    CKP(p, cudaStreamSynchronize(s));  // hbase is reused by the next segment
-    float t1 = 0.f, t2 = 0.f;
-    cudaEventElapsedTime(&t1, ev[2], ev[3]);
-    cudaEventElapsedTime(&t2, ev[3], ev[0]);
-    t_rec += t1;
-    t_adj += t2;
+    CKP(p, cudaEventRecord(evA[j], sa));
+    nn_adj += cnt;
+    // meanwhile recompute segment j-1 into the slot set segment j+1 used
+    if (j > 0) {
+      if (j + 1 < nck) CKP(p, cudaStreamWaitEvent(sr, evA[j + 1], 0));
+      if ((st_ = recompute(j - 1)) != SHM_OK) return st_;
+    }
+  }
+  cudaEventRecord(ev_end_r, sr);
+  cudaEventRecord(ev_end_a, sa);
+  CKP(p, cudaStreamWaitEvent(s, ev_end_r, 0));
+  CKP(p, cudaStreamWaitEvent(s, ev_end_a, 0));
+  CKP(p, cudaStreamSynchronize(s));
+  cudaEventElapsedTime(&t_rec, ev[2], ev_end_r);
+  cudaEventElapsedTime(&t_adj, ev[3], ev_end_a);
+  cudaEventDestroy(ev_s);
+  cudaEventDestroy(ev_end_r);
+  cudaEventDestroy(ev_end_a);
+  for (int j = 0; j < nck; ++j) {
+    cudaEventDestroy(evR[j]);
+    cudaEventDestroy(evA[j]);
   }
   for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   p->fb_ms[0] = t_fwd;
