@@ -26,10 +26,11 @@ struct PlateDesc {
   double sx, sy, area4;
 };
 
-// task: plate, strip, block, first force entry, force count
+// task: plate, strip, block, rows, first force entry, force count, first
+// point-output entry, point-output count (the outputs the task's update owns)
 struct TaskDesc {
   int plate, strip, block, nrows;
-  int f0, fn, pad0, pad1;
+  int f0, fn, o0, on;
 };
 
 template <typename T> struct StructArgs {

@@ -91,11 +91,21 @@ struct F32Args {
   float a0, a1, blowup;
   int* flag;
   const int* d_base;
+  // adjoint step (kAdj): residual forces at the point outputs each task owns,
+  // forward state u_{n-1} for the damage gradient, gradient in plan order
+  const int* __restrict__ o_xl;
+  const int* __restrict__ o_iy;
+  const int* __restrict__ o_field;
+  const int* __restrict__ o_q;
+  const double* __restrict__ asig;  // [nout][nft] residuals in reversed time
+  const float* __restrict__ um;
+  double* grad;
+  const int* __restrict__ e_of_g;   // grid-order element -> plan element
 };
 
 // per-group task facts, uniform inside the group
 struct GroupTask {
-  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, scen;
+  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, scen, o0, on;
   long long node0, egrid0;
   float sx, sy, area4;
 };
@@ -116,6 +126,8 @@ __device__ __forceinline__ GroupTask load_group_task(const F32Args& a, int tid) 
   t.NX = pl.NX;
   t.f0 = tk.f0;
   t.fn = tk.fn;
+  t.o0 = tk.o0;
+  t.on = tk.on;
   t.scen = pl.scen;
   t.node0 = pl.node0;
   t.egrid0 = pl.egrid0;
@@ -160,7 +172,11 @@ __device__ __forceinline__ void ring_load(float* ring, const float* __restrict__
   }
 }
 
-template <int EW, bool kSensor>
+// kAdj: the adjoint step of the same operator (K symmetric): lambda in
+// place of u, residual forces r(n) at the point outputs instead of the
+// excitation, and dJ/dd_e -= lambda_n' K_e^0 u_{n-1} accumulated per element
+// (FP32 line products, FP64 per-element and across-step sums).
+template <int EW, bool kSensor, bool kAdj = false>
 __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, int kstep) {
   using GM = F32Geom<EW>;
   constexpr int G = GM::G;
@@ -309,9 +325,14 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         float2 L[LAMP];
         {
           const float2* mp = a.matp + (int64_t)a.emat_g[egrid] * LAMP;
-          const float2 kp = bc2(a.ekeep_g[egrid]);
+          if constexpr (kAdj) {  // K_e^0: the stiffness factor is applied to the line's forces
 #pragma unroll
-          for (int c = 0; c < LAMP; ++c) L[c] = mul2(mp[c], kp);
+            for (int c = 0; c < LAMP; ++c) L[c] = mp[c];
+          } else {
+            const float2 kp = bc2(a.ekeep_g[egrid]);
+#pragma unroll
+            for (int c = 0; c < LAMP; ++c) L[c] = mul2(mp[c], kp);
+          }
         }
         float2 Fe2[5][3];
 #pragma unroll
@@ -429,6 +450,20 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             out[f][2 * p + 1] = o2[p].y;
           }
         }
+        if constexpr (kAdj) {
+          // line j's share of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
+          const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
+          const float keep = a.ekeep_g[egrid];
+          float dl = 0.f;
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+              dl += out[f][i] * umr[f * a.nnode_pad + i];
+              out[f][i] *= keep;
+            }
+          vred[j * CTA_ELEMS + lane] = dl;
+        }
       } else {
 #pragma unroll
         for (int f = 0; f < 5; ++f)
@@ -466,6 +501,12 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         __syncthreads();
       }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
+      if (kAdj && j == 0 && valid && owned_row && q > 0) {
+        double sum = 0.0;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
+        a.grad[a.e_of_g[egrid]] -= sum;
+      }
       if (kSensor && j == 0 && valid && owned_row && q > 0) {
         const int sl = a.esens_g[egrid];
         if (sl >= 0) {
@@ -490,7 +531,17 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
           for (int f = 0; f < 5; ++f) F[f] = bnd[f * W];
           const GroupTask& t2 = pick<G>(gt, gg);
-          if (t2.fn > 0) {
+          if (kAdj && t2.on > 0) {
+            const int iy = 5 * (t2.eyA + r) + j;
+            for (int oi = t2.o0; oi < t2.o0 + t2.on; ++oi)
+              if (a.o_iy[oi] == iy && a.o_xl[oi] == 5 + c) {
+                const float rv = (float)a.asig[(int64_t)a.o_q[oi] * a.nft + (nn - 1)];
+#pragma unroll
+                for (int f = 0; f < 5; ++f)
+                  if (f == a.o_field[oi]) F[f] += rv;
+              }
+          }
+          if (!kAdj && t2.fn > 0) {
             const int iy = 5 * (t2.eyA + r) + j;
             for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)
               if (a.f_iy[fi] == iy && a.f_xl[fi] == 5 + c) {

@@ -338,11 +338,14 @@ struct StructPlan {
   int* esens_g = nullptr;
   int *f_xl = nullptr, *f_iy = nullptr, *f_field = nullptr;
   double* f_val = nullptr;
+  int *o_xl = nullptr, *o_iy = nullptr, *o_field = nullptr, *o_q = nullptr;  // point outputs per task
+  int* e_of_g = nullptr;   // grid-order element -> plan element
   float2* matp = nullptr;  // FP32 packed laminate pairs [nmat][LAMP]
   // host copies kept for re-planning the task list (autotuner)
   std::vector<PlateDesc> h_plates;
   std::vector<int> h_fscen, h_fnode, h_ffield;
   std::vector<double> h_fval;
+  std::vector<int> h_oscen, h_onode, h_ofield, h_oq;
   std::vector<void*> task_allocs;
 };
 
@@ -700,6 +703,10 @@ static shm_status set_func_attrs(shm_plan* p) {
                               (int)struct_f32_smem_bytes<16>()));
   CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_f32_smem_bytes<16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<32, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<16>()));
   return SHM_OK;
 }
 
@@ -737,6 +744,7 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     TaskDesc t;
     std::vector<int> fxl, fiy, ffield;
     std::vector<double> fval;
+    std::vector<int> oxl, oiy, ofield, oq;
   };
   const int nscen = (int)sp.h_plates.size();
   std::vector<TaskTmp> tasks;
@@ -748,7 +756,7 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     for (int b = 0; b < nb; ++b)
       for (int k = 0; k < ns; ++k) {
         TaskTmp t;
-        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};
+        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};  // rows, forces and outputs set below
         const int last = std::min(H * (b + 1), pl.ney);
         t.t.nrows = b == 0 ? last : last - (H * b - 1);
         task_index[s][(size_t)b * ns + k] = (int)tasks.size();
@@ -769,12 +777,32 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     t.ffield.push_back(sp.h_ffield[q]);
     t.fval.push_back(sp.h_fval[q]);
   }
+  for (size_t q = 0; q < sp.h_onode.size(); ++q) {  // point outputs: the task that updates the node
+    const int s = sp.h_oscen[q];
+    const PlateDesc& pl = sp.h_plates[s];
+    const int ns = (pl.NX + own - 1) / own, nb = (pl.ney + H - 1) / H;
+    const int node = sp.h_onode[q];
+    const int ix = node % pl.NX, iy = node / pl.NX;
+    const int k = ix / own;
+    const int b = std::min(iy / (5 * H), nb - 1);
+    TaskTmp& t = tasks[task_index[s][(size_t)b * ns + k]];
+    t.oxl.push_back(ix - 5 * (k * (EW - 1) - 1));
+    t.oiy.push_back(iy);
+    t.ofield.push_back(sp.h_ofield[q]);
+    t.oq.push_back(sp.h_oq[q]);
+  }
   // longest tasks first so that lane groups of a CTA stay in step
   std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
   std::vector<TaskDesc> td;
-  std::vector<int> fxl, fiy, ffield;
+  std::vector<int> fxl, fiy, ffield, oxl, oiy, ofield, oq;
   std::vector<double> fval;
   for (TaskTmp& t : tasks) {
+    t.t.o0 = (int)oxl.size();
+    t.t.on = (int)t.oxl.size();
+    oxl.insert(oxl.end(), t.oxl.begin(), t.oxl.end());
+    oiy.insert(oiy.end(), t.oiy.begin(), t.oiy.end());
+    ofield.insert(ofield.end(), t.ofield.begin(), t.ofield.end());
+    oq.insert(oq.end(), t.oq.begin(), t.oq.end());
     t.t.f0 = (int)fxl.size();
     t.t.fn = (int)t.fxl.size();
     fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
@@ -797,7 +825,11 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
   if ((st = upload(p, &sp.f_iy, fiy)) != SHM_OK) return st;
   if ((st = upload(p, &sp.f_field, ffield)) != SHM_OK) return st;
   if ((st = upload(p, &sp.f_val, fval)) != SHM_OK) return st;
-  sp.task_allocs = {dt, sp.f_xl, sp.f_iy, sp.f_field, sp.f_val};
+  if ((st = upload(p, &sp.o_xl, oxl)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.o_iy, oiy)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.o_field, ofield)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.o_q, oq)) != SHM_OK) return st;
+  sp.task_allocs = {dt, sp.f_xl, sp.f_iy, sp.f_field, sp.f_val, sp.o_xl, sp.o_iy, sp.o_field, sp.o_q};
   sp.tasks = dt;
   sp.ntask = (int)td.size();
   sp.tile = EW;
@@ -820,7 +852,7 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
   const int64_t FP = p->fen_pad;
   std::vector<PlateDesc> plates(nscen);
   int64_t egrid = 0;
-  std::vector<int> emat_g(p->fen), esens_g(p->fen, -1);
+  std::vector<int> emat_g(p->fen), esens_g(p->fen, -1), e_of_g(p->fen, 0);
   std::vector<double> ekeep_g(p->fen, 1.0);
   for (int s = 0; s < nscen; ++s) {
     const shm_mesh& m = meshes[s];
@@ -861,6 +893,7 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
       emat_g[egrid + (int64_t)ey * nex + ex] = emat[ge];
       ekeep_g[egrid + (int64_t)ey * nex + ex] = ekeep[ge];
       esens_g[egrid + (int64_t)ey * nex + ex] = esens[ge];
+      e_of_g[egrid + (int64_t)ey * nex + ex] = (int)ge;
     }
     plates[s] = PlateDesc{nex, ney, NX, s, (long long)p->node_off[s], (long long)egrid, sx, sy, a4};
     egrid += (int64_t)nex * ney;
@@ -874,6 +907,14 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
       sp.h_ffield.push_back((d - 1) % 5);
       sp.h_fval.push_back(runs[sidx].force_val[q]);
     }
+  for (int sidx = 0; sidx < nscen; ++sidx)
+    for (int q = 0; q < runs[sidx].n_out; ++q) {
+      const int d = runs[sidx].out_dof[q];
+      sp.h_oscen.push_back(sidx);
+      sp.h_onode.push_back((d - 1) / 5);
+      sp.h_ofield.push_back((d - 1) % 5);
+      sp.h_oq.push_back(p->out_off[sidx] + q);
+    }
   int EW = tile_elems;
   if (EW != 16 && EW != 32) EW = lane_utilisation(meshes, nscen, 32) >= 0.9 * lane_utilisation(meshes, nscen, 16) ? 32 : 16;
   shm_status st;
@@ -885,6 +926,7 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
   if ((st = struct_tasks(p, EW, rows_per_block > 0 ? rows_per_block : 16)) != SHM_OK) return st;
   if ((st = upload(p, &sp.emat_g, emat_g)) != SHM_OK) return st;
   if ((st = upload(p, &sp.esens_g, esens_g)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.e_of_g, e_of_g)) != SHM_OK) return st;
   if (p->prec == 64) {
     double* k = nullptr;
     if ((st = upload(p, &k, ekeep_g)) != SHM_OK) return st;
@@ -907,9 +949,9 @@ static shm_status struct_build(shm_plan* p, int nscen, const shm_mesh* meshes, c
   return SHM_OK;
 }
 
-static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s) {
+static F32Args struct_f32_args(shm_plan* p) {
   StructPlan& sp = p->sp;
-  F32Args a;
+  F32Args a{};
   a.plates = sp.plates;
   a.tasks = sp.tasks;
   a.ntask = sp.ntask;
@@ -947,6 +989,17 @@ static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s
   a.blowup = (float)p->blowup;
   a.flag = p->flag;
   a.d_base = p->d_base;
+  a.o_xl = sp.o_xl;
+  a.o_iy = sp.o_iy;
+  a.o_field = sp.o_field;
+  a.o_q = sp.o_q;
+  a.e_of_g = sp.e_of_g;
+  return a;
+}
+
+static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s) {
+  StructPlan& sp = p->sp;
+  F32Args a = struct_f32_args(p);
   const bool sens = p->nslot > 0;
   if (sp.tile == 32) {
     if (sens)
@@ -1846,6 +1899,20 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   a.nout = 0;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
+  // plans on the fused FP32 kernel step the adjoint with its adjoint variant
+  const bool fused = sizeof(T) == 4 && p->path == 2 && !p->sp_generic;
+  F32Args af{};
+  if (fused) {
+    af = struct_f32_args(p);
+    af.UA = (float*)p->LA;
+    af.UB = (float*)p->LB;
+    af.outp = nullptr;
+    af.d_base = p->d_base_adj;
+    af.nout = 0;
+    af.fs.frm_int = 0;
+    af.asig = p->asig;
+    af.grad = p->grad;
+  }
   auto seg_state = [&](int j, int i) -> T* {  // u at forward time sj + i of segment j
     T* ck_u = ck + (size_t)j * 2 * S;
     if (i < 0) return ck_u + S;
@@ -1879,9 +1946,18 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     // adjoint through segment j once its states exist
     CKP(p, cudaStreamWaitEvent(sa, evR[j], 0));
     for (int kk = 0; kk < cnt; ++kk) {
-      a.um = seg_state(j, N + n0 - (nn_adj + kk) - sj);  // u at forward time N + n0 - nn
-      k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, sa>>>(a, kk);
-      k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, sa>>>(a, kk);
+      const T* um = seg_state(j, N + n0 - (nn_adj + kk) - sj);  // u at forward time N + n0 - nn
+      if (fused) {
+        af.um = (const float*)um;
+        if (p->sp.tile == 32)
+          k_struct_step_f32<32, false, true><<<p->sp.grid, CTA_THREADS, struct_f32_smem_bytes<32>(), sa>>>(af, kk);
+        else
+          k_struct_step_f32<16, false, true><<<p->sp.grid, CTA_THREADS, struct_f32_smem_bytes<16>(), sa>>>(af, kk);
+      } else {
+        a.um = um;
+        k_elem_adjoint<T><<<nblk, CTA_THREADS, smem, sa>>>(a, kk);
+        k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, sa>>>(a, kk);
+      }
     }
     k_advance<<<1, 1, 0, sa>>>(p->d_base_adj, cnt);
     CKP(p, cudaGetLastError());
