@@ -187,6 +187,12 @@ shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *
 /* Device time (ms, CUDA events) of the last shm_forward_backward's phases:
  * [0] forward pass with checkpoints, [1] segment recomputes, [2] adjoint steps. */
 shm_status shm_forward_backward_timing(const shm_plan *plan, float *ms3);
+/* Device memory that shm_forward_backward may use to keep every state of the
+ * last checkpoint segments of the forward pass (those segments are not
+ * recomputed): max_bytes -1 = the device's spare memory less 8 GiB (default),
+ * 0 = recompute every segment; values below -1 leave the setting unchanged.
+ * last_segments (may be NULL) receives the number of segments the last call kept. */
+shm_status shm_set_adjoint_store(shm_plan *plan, int64_t max_bytes, int32_t *last_segments);
 
 /* Autotuner for plans on the structured path: times `steps` steps of the
  * general kernels and of every (elements per lane group, element rows per

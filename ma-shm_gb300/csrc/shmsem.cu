@@ -394,6 +394,8 @@ struct shm_plan {
   // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
   float fb_ms[3] = {0.f, 0.f, 0.f};  // last forward_backward: forward, recompute, adjoint (ms)
+  int64_t store_cap = -1;             // bytes for states kept by the forward pass (-1 = spare memory)
+  int last_nstore = 0;
   double *grad = nullptr, *asig = nullptr;
   int* d_base_adj = nullptr;
   int seg_k = 0, nck = 0;
@@ -1824,6 +1826,28 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   cudaEvent_t ev[4];
   for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
   float t_rec = 0.f, t_adj = 0.f;
+  // the last `nstore` segments keep every state of the forward pass in spare
+  // device memory (8 GiB left free), so the backward pass recomputes only the
+  // others
+  int nstore = 0;
+  T* store = nullptr;
+  {
+    size_t fr = 0, tot = 0;
+    const size_t per = (size_t)k * SB;
+    if (p->store_cap >= 0) {
+      nstore = (int)std::min<size_t>((size_t)nck, (size_t)p->store_cap / per);
+    } else if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+      const size_t margin = (size_t)8 << 30;
+      if (fr > margin + per) nstore = (int)std::min<size_t>((size_t)nck, (fr - margin) / per);
+    }
+    while (nstore > 0 && cudaMalloc(&store, (size_t)nstore * k * SB) != cudaSuccess) {
+      cudaGetLastError();
+      nstore /= 2;
+    }
+  }
+  const int jstore = nck - nstore;  // first stored segment
+  p->last_nstore = nstore;
+  auto stored = [&](int j, int i) -> T* { return store + ((size_t)(j - jstore) * k + (i - 1)) * S; };
   // 1. forward pass with the plan's own step kernels (the structured fused
   // kernel when the plan uses it), checkpoint (u_n, u_{n-1}) every k steps
   if ((st_ = shm_reset(p)) != SHM_OK) return st_;
@@ -1831,10 +1855,39 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   cudaEventRecord(ev[0], s);
   for (int j = 0; j < nck; ++j) {
     const int n = n0 + j * k;
-    const bool odd = ((n - n0) & 1);
-    CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S, odd ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
-    CKP(p, cudaMemcpyAsync(ck + (size_t)j * 2 * S + S, odd ? UA : UB, SB, cudaMemcpyDeviceToDevice, s));
-    if ((st_ = advance_async(p, std::min(k, N - n + 1), s)) != SHM_OK) return st_;
+    const int cnt = std::min(k, N - n + 1);
+    T* cku = ck + (size_t)j * 2 * S;
+    if (j <= jstore) {  // the states are in the ping-pong pair
+      const bool odd = ((n - n0) & 1);
+      CKP(p, cudaMemcpyAsync(cku, odd ? UB : UA, SB, cudaMemcpyDeviceToDevice, s));
+      CKP(p, cudaMemcpyAsync(cku + S, odd ? UA : UB, SB, cudaMemcpyDeviceToDevice, s));
+    }
+    if (j < jstore) {
+      if ((st_ = advance_async(p, cnt, s)) != SHM_OK) return st_;
+      continue;
+    }
+    // stored segment: step i reads state i (and i-1), writes state i+1 into
+    // the store; its last step writes the next checkpoint
+    k_set<<<1, 1, 0, s>>>(p->d_base, n);
+    for (int i = 0; i < cnt; ++i) {
+      T* cur = i == 0 ? cku : stored(j, i);
+      T* prv = i == 0 ? cku + S : (i == 1 ? cku : stored(j, i - 1));
+      T* out = i + 1 < cnt ? stored(j, i + 1) : (j + 1 < nck ? ck + (size_t)(j + 1) * 2 * S : UA);
+      const bool odd = ((n + i - n0) & 1);
+      p->ov_UA = odd ? prv : cur;
+      p->ov_UB = odd ? cur : prv;
+      p->ov_out = out;
+      cudaError_t e = launch_step(p, i, s);
+      p->ov_UA = p->ov_UB = p->ov_out = nullptr;
+      if (e != cudaSuccess) {
+        if (store) cudaFree(store);
+        p->err = std::string("forward: ") + cudaGetErrorString(e);
+        return SHM_ERR_CUDA;
+      }
+    }
+    if (j + 1 < nck)  // u_{n-1} of the next checkpoint
+      CKP(p, cudaMemcpyAsync(ck + (size_t)(j + 1) * 2 * S + S, cnt > 1 ? stored(j, cnt - 1) : cku, SB,
+                             cudaMemcpyDeviceToDevice, s));
   }
   cudaEventRecord(ev[1], s);
   // 2. misfit (FP64) and the residuals in reversed time
@@ -1917,10 +1970,15 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     T* ck_u = ck + (size_t)j * 2 * S;
     if (i < 0) return ck_u + S;
     if (i == 0) return ck_u;
+    if (j >= jstore) return stored(j, i);
     return seg + ((size_t)(j & 1) * (k + 1) + i) * S;
   };
   cudaEventRecord(ev[2], sr);
   auto recompute = [&](int j) -> shm_status {
+    if (j >= jstore) {  // states kept by the forward pass
+      CKP(p, cudaEventRecord(evR[j], sr));
+      return SHM_OK;
+    }
     const int sj = n0 + j * k, cnt = std::min(sj + k - 1, N) - sj + 1;
     k_set<<<1, 1, 0, sr>>>(p->d_base, sj);
     for (int i = 0; i + 1 < cnt; ++i) {
@@ -1976,6 +2034,7 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   CKP(p, cudaStreamSynchronize(s));
   cudaEventElapsedTime(&t_rec, ev[2], ev_end_r);
   cudaEventElapsedTime(&t_adj, ev[3], ev_end_a);
+  if (store) cudaFree(store);
   cudaEventDestroy(ev_s);
   cudaEventDestroy(ev_end_r);
   cudaEventDestroy(ev_end_a);
@@ -2004,6 +2063,13 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
 extern "C" shm_status shm_forward_backward_timing(const shm_plan* p, float* ms3) {
   if (!p || !ms3) return SHM_ERR_BAD_ARG;
   for (int i = 0; i < 3; ++i) ms3[i] = p->fb_ms[i];
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_set_adjoint_store(shm_plan* p, int64_t max_bytes, int32_t* last_segments) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (last_segments) *last_segments = p->last_nstore;
+  if (max_bytes >= -1) p->store_cap = max_bytes;
   return SHM_OK;
 }
 

@@ -86,6 +86,7 @@ SIGNATURES = {
                                         C.POINTER(ShmRun), C.POINTER(ShmOptions), C.POINTER(C.c_void_p)]),
     "shm_forward_backward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_int32, C.c_void_p]),
     "shm_forward_backward_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "shm_set_adjoint_store": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
     "shm_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_float)]),
     "shm_stiffness_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

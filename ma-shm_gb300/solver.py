@@ -111,6 +111,20 @@ class Plan:
             e0 += fen
         return mis, out
 
+    def set_adjoint_store(self, max_bytes: int | None = None) -> int:
+        """Bytes forward_backward may keep for the last segments' states
+        (None: the device's spare memory; 0: recompute every segment).
+        Returns the number of segments the previous call kept."""
+        n = C.c_int32()
+        self._check(self.lib.shm_set_adjoint_store(self.handle, -1 if max_bytes is None else int(max_bytes),
+                                                   C.byref(n)))
+        return n.value
+
+    def stored_segments(self) -> int:
+        n = C.c_int32()
+        self._check(self.lib.shm_set_adjoint_store(self.handle, -2, C.byref(n)))
+        return n.value
+
     def forward_backward_timing(self) -> dict:
         """Device ms of the last forward_backward's forward pass, segment
         recomputes and adjoint steps."""

@@ -124,10 +124,33 @@ def test_adjoint_on_structured_plan(pkg, prec):
     for path in (1, 2):
         plan = pkg.Plan([sc], run, precision=prec, path=path)
         assert plan.info["path"] == path
+        plan.set_adjoint_store(0)  # recompute every segment
         res[path] = plan.forward_backward([target], ckpt_every=37)
+        assert plan.stored_segments() == 0
         t = plan.forward_backward_timing()
         assert t["forward_ms"] > 0 and t["recompute_ms"] > 0 and t["adjoint_ms"] > 0
         plan.close()
     tol = 1e-10 if prec == 64 else 1e-4
     assert rel(res[2][1][0], res[1][1][0]) <= tol
     assert abs(res[2][0][0] - res[1][0][0]) <= tol * res[1][0][0]
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_adjoint_stored_segments_equal_recompute(pkg, path):
+    """Keeping the last segments' forward states instead of recomputing them
+    changes nothing: the states are the same bits."""
+    sc, run, target = adjoint_case(pkg, seed=5)
+    plan = pkg.Plan([sc], run, precision=32, path=path)
+    k = 30
+    nck = -(-(run.nft - run.nn_first + 1) // k)
+    state_bytes = 4 * 5 * plan.info["nnode"]
+    got = {}
+    for name, cap in (("none", 0), ("part", (nck // 2) * k * state_bytes), ("all", None)):
+        plan.set_adjoint_store(cap)
+        got[name] = plan.forward_backward([target], ckpt_every=k)
+        got[name + "_n"] = plan.stored_segments()
+    plan.close()
+    assert got["none_n"] == 0 and 0 < got["part_n"] < nck and got["all_n"] == nck
+    for name in ("part", "all"):
+        np.testing.assert_array_equal(got[name][1][0], got["none"][1][0])
+        assert got[name][0][0] == got["none"][0][0]
