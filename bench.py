@@ -193,6 +193,7 @@ def adjoint_bench(pkg, args):
         torch.cuda.synchronize()
         t_adj[path] = time.perf_counter() - t0
         out[f"phases_ms_path{path}"] = p.forward_backward_timing()
+        out[f"stored_segments_path{path}"] = p.stored_segments()
         p.close()
     g32 = grads[2]
     out["forward_s_general_path"] = times[1]
