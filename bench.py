@@ -29,6 +29,10 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 ALG_BYTES = {32: 16.0, 64: 32.0}   # algorithmic bytes per DOF-step (u_n, u_n-1, u_n+1, 1/M)
+# DRAM bytes (read + write) per DOF of one k_struct_step_f32 launch, from the ncu
+# capture in profiles/k_struct_step_f32_batch64_v3.md (292.9 + 82.4 MB for the
+# 64-plate batch of 30 001 270 DOF); traffic grows with the DOF count
+F32_TRAFFIC_PER_DOF = (292.910336e6 + 82.395648e6) / 30001270
 METRIC = "DOF-steps/s (batched flat-shell SEM forward, 512 uneven plates)"
 
 
@@ -434,7 +438,10 @@ def main():
     pk, pk_kind = peaks()
     achieved = ALG_BYTES[args.precision] * ndof / per_launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / pk["hbm_gbs"], "traffic": None,
+            "frac": achieved / pk["hbm_gbs"],
+            "traffic": (F32_TRAFFIC_PER_DOF * ndof if args.precision == 32 and plan.info["path"] == 2 else None),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 64-plate "
+                              "batch, scaled by DOF (bytes per launch)",
             "basis": f"{ALG_BYTES[args.precision]:.0f} B/DOF-step x {ndof} DOF per launch of "
                      f"k_struct_step, CUDA events over {args.steps} launches; peak {pk_kind}"}
     launches = args.steps * plan.info["launches_per_step"] + (args.steps // args.graph if args.graph else 1)

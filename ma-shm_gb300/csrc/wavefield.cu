@@ -21,7 +21,8 @@
 //
 // Per frame (device, k_grid): one thread per grid point, all frames in a loop;
 // the owner's 36 node values of the requested motion (1..9, lever +-h/2 for
-// the top/bottom surface, :281-510) are combined with the tensor-product
+// the top/bottom surface, :281-510; the motion is a template parameter, the
+// arithmetic the frames' precision) are combined with the tensor-product
 // Lagrange weights l_i(ksi) l_j(eta), the functions shape2Dp.m evaluates
 // through the inverse 2D Vandermonde matrix.  The top-surface rule
 // U(nodes_under) = U(nodes_above) (:512-515) is a node remap baked into the
@@ -78,75 +79,79 @@ struct Lagrange {
   }
 };
 
-__device__ __forceinline__ void lagrange_dev(double t, double* l) {
+template <typename TC>
+__device__ __forceinline__ void lagrange_dev(double t, TC* l) {
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
     double p = c_lw[i];
 #pragma unroll
     for (int m = 0; m < NP; ++m)
       if (m != i) p *= (t - c_gx[m]);
-    l[i] = p;
+    l[i] = (TC)p;
   }
 }
 
-// value of motion type m (1..9) at one node; fields f_* are offsets of the
-// field planes (or -1 when unused); hs = +h/2 (top) or -h/2 (bottom)
-template <typename TF>
-__device__ __forceinline__ double motion_value(const TF* __restrict__ fr, int64_t node, int m, int64_t oux,
-                                               int64_t ofx, int64_t ouy, int64_t ofy, int64_t ouz, double hs) {
-  switch (m) {
-    case 1: return (double)fr[oux + node];
-    case 2: return (double)fr[ouy + node];
-    case 3: return (double)fr[ouz + node];
-    case 4: return (double)fr[ofx + node];
-    case 5: return (double)fr[ofy + node];
-    case 6: return (double)fr[oux + node] + hs * (double)fr[ofx + node];
-    case 7: return (double)fr[ouy + node] + hs * (double)fr[ofy + node];
-    case 8: {
-      const double a = (double)fr[oux + node] + hs * (double)fr[ofx + node];
-      const double b = (double)fr[ouy + node] + hs * (double)fr[ofy + node];
-      return sqrt(a * a + b * b);
-    }
-    default: {
-      const double a = (double)fr[oux + node] + hs * (double)fr[ofx + node];
-      const double b = (double)fr[ouy + node] + hs * (double)fr[ofy + node];
-      const double c = (double)fr[ouz + node];
-      return sqrt(a * a + b * b + c * c);
-    }
+// value of motion type M (1..9) at one node; o* are offsets of the field
+// planes; hs = +h/2 (top) or -h/2 (bottom)
+template <int M, typename TF, typename TC>
+__device__ __forceinline__ TC motion_value(const TF* __restrict__ fr, int64_t node, int64_t oux, int64_t ofx,
+                                           int64_t ouy, int64_t ofy, int64_t ouz, TC hs) {
+  if constexpr (M == 1) return (TC)fr[oux + node];
+  if constexpr (M == 2) return (TC)fr[ouy + node];
+  if constexpr (M == 3) return (TC)fr[ouz + node];
+  if constexpr (M == 4) return (TC)fr[ofx + node];
+  if constexpr (M == 5) return (TC)fr[ofy + node];
+  if constexpr (M == 6) return (TC)fr[oux + node] + hs * (TC)fr[ofx + node];
+  if constexpr (M == 7) return (TC)fr[ouy + node] + hs * (TC)fr[ofy + node];
+  if constexpr (M == 8) {
+    const TC a = (TC)fr[oux + node] + hs * (TC)fr[ofx + node];
+    const TC b = (TC)fr[ouy + node] + hs * (TC)fr[ofy + node];
+    return sqrt(a * a + b * b);
   }
+  if constexpr (M == 9) {
+    const TC a = (TC)fr[oux + node] + hs * (TC)fr[ofx + node];
+    const TC b = (TC)fr[ouy + node] + hs * (TC)fr[ofy + node];
+    const TC c = (TC)fr[ouz + node];
+    return sqrt(a * a + b * b + c * c);
+  }
+  return TC(0);
 }
 
 // Data[n][p] = sum_{j,i} l_j(eta_p) l_i(ksi_p) value(node(owner_p, j*6+i)) for
-// every frame n; frames fr[n*frame_stride + field_offset + node]
-template <typename TF>
-__global__ void __launch_bounds__(GRID_THREADS) k_grid(const int* __restrict__ owner,
+// every frame n; frames fr[n*frame_stride + field_offset + node].  TC is the
+// arithmetic type: the frames' own precision (FP32 frames are combined in
+// FP32, FP64 frames in FP64).
+template <int M, typename TF, typename TC>
+__global__ void __launch_bounds__(GRID_THREADS, 2) k_grid(const int* __restrict__ owner,
                                                         const double2* __restrict__ ke,
                                                         const int* __restrict__ conn, int fen_search, int64_t npts,
                                                         const TF* __restrict__ fr, int64_t frame_stride,
                                                         int64_t oux, int64_t ofx, int64_t ouy, int64_t ofy,
-                                                        int64_t ouz, int motion, double hs, int nframes,
+                                                        int64_t ouz, double hs, int nframes,
                                                         double* __restrict__ out) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npts) return;
   const int e = owner[p];
   const double2 q = ke[p];
-  double lx[NP], ly[NP];
+  TC lx[NP], ly[NP];
   lagrange_dev(q.x, lx);
   lagrange_dev(q.y, ly);
   int nid[NPE];
 #pragma unroll
   for (int k = 0; k < NPE; ++k) nid[k] = conn[(int64_t)k * fen_search + e];
+  const TC hsc = (TC)hs;
   for (int n = 0; n < nframes; ++n) {
     const TF* f = fr + (int64_t)n * frame_stride;
-    double acc = 0.0;
+    TC acc = TC(0);
 #pragma unroll
     for (int j = 0; j < NP; ++j) {
-      double row = 0.0;
+      TC row = TC(0);
 #pragma unroll
-      for (int i = 0; i < NP; ++i) row += lx[i] * motion_value(f, nid[j * NP + i], motion, oux, ofx, ouy, ofy, ouz, hs);
+      for (int i = 0; i < NP; ++i)
+        row += lx[i] * motion_value<M, TF, TC>(f, nid[j * NP + i], oux, ofx, ouy, ofy, ouz, hsc);
       acc += ly[j] * row;
     }
-    out[(int64_t)n * npts + p] = acc;
+    out[(int64_t)n * npts + p] = (double)acc;
   }
 }
 
@@ -456,14 +461,30 @@ extern "C" shm_status shm_grid_points(const shm_grid* g, double* xp, double* yp,
   return SHM_OK;
 }
 
+template <int M, typename TF>
+static void launch_grid_m(shm_grid* g, const TF* fr, int64_t frame_stride, const int64_t off[5], double hs,
+                          int nframes, double* d_out, cudaStream_t s) {
+  const int64_t nblk = (g->npts + GRID_THREADS - 1) / GRID_THREADS;
+  k_grid<M, TF, TF><<<(unsigned)nblk, GRID_THREADS, 0, s>>>(g->d_owner, g->d_ke, g->d_conn, g->fen_search,
+                                                            g->npts, fr, frame_stride, off[0], off[1], off[2],
+                                                            off[3], off[4], hs, nframes, d_out);
+}
+
 template <typename TF>
 static shm_status launch_grid(shm_grid* g, const TF* fr, int64_t frame_stride, const int64_t off[5], int motion,
                               double hs, int nframes, double* d_out, cudaStream_t s) {
   if (nframes <= 0) return SHM_OK;
-  const int64_t nblk = (g->npts + GRID_THREADS - 1) / GRID_THREADS;
-  k_grid<TF><<<(unsigned)nblk, GRID_THREADS, 0, s>>>(g->d_owner, g->d_ke, g->d_conn, g->fen_search, g->npts, fr,
-                                                     frame_stride, off[0], off[1], off[2], off[3], off[4], motion,
-                                                     hs, nframes, d_out);
+  switch (motion) {
+    case 1: launch_grid_m<1>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 2: launch_grid_m<2>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 3: launch_grid_m<3>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 4: launch_grid_m<4>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 5: launch_grid_m<5>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 6: launch_grid_m<6>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 7: launch_grid_m<7>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    case 8: launch_grid_m<8>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+    default: launch_grid_m<9>(g, fr, frame_stride, off, hs, nframes, d_out, s); break;
+  }
   GCK(g, cudaGetLastError());
   return SHM_OK;
 }
