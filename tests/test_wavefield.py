@@ -140,3 +140,46 @@ def test_interpolation_from_plan_frames(pkg, precision):
                 assert rel(got, np.transpose(want, (2, 0, 1))) <= tols[kind], (surface, fv, motion)
         g.close()
     plan.close()
+
+
+@pytest.mark.gpu
+def test_reference_entry_points_write_frames_and_grid(pkg, tmp_path):
+    """main_flat_shell writes the reference's frame files for field_variable
+    'all' (15 per frame), spec2meshgrid_flat_shell reads them back and writes
+    Data(Ny, Nx, nFrames); both match the oracle."""
+    from scipy.io import loadmat
+    M = pkg.materials
+    mesh = pkg.mesh.structured_plate(0.06, 0.06, 6, 6)
+    q = M.ply_stiffness(**M.CFRP_PLY)
+    lam = M.laminate(q, M.CFRP_RHO, M.CFRP_PLY_T, M.CFRP_ANGLES)
+    nft = 240
+    dt = pkg.element.stable_dt([pkg.element.rect_nodes(0.01, 0.01)], [lam])
+    inputs = dict(nft=nft, tt=dt * nft, f_1=50e3, f_2=250e3, t_1=0.0, nFrames=4, field_variable="all",
+                  etad_xy=4e2, etad_z=4e3, V0=1.0, lh=np.array(M.CFRP_PLY_T), mat_table=M.table_row(lam))
+    out = tmp_path / "out"
+    tf = pkg.main_flat_shell(7, inputs, mesh, "gpu", str(out), precision=64)
+    assert len(tf) == 4 and np.all(np.diff(tf) > 0)
+    names = [p + c for p in "UVA" for c in ("x", "Fix", "y", "Fiy", "z")]
+    for c in range(1, 5):
+        for nm in names:
+            v = loadmat(out / f"{nm}_frame{c}.mat")[nm]
+            assert v.shape == (mesh["coords"].shape[0], 1)
+    # oracle frames of the same run
+    from oracle.oracle import OracleProblem
+    orc = OracleProblem(mesh["nodes"], mesh["coords"], M.table_row(lam)[None, :])
+    centre = pkg.mesh.nearest_node(mesh["coords"], 0.03, 0.03)
+    _, st = pkg.hanning_signal(dt, nft, 50e3, 250e3, 0.0)
+    ref = orc.run(dt, nft, st, nn_first=2, eta_xy=4e2, eta_z=4e3, force_dof=[5 * centre], force_val=[1.0],
+                  out_dof=[5 * centre], h=float(np.sum(M.CFRP_PLY_T)), frm_int=nft // 4, frame_dof=0, frame_kind=3)
+    for c in range(4):
+        for k, nm in enumerate(names):
+            got = loadmat(out / f"{nm}_frame{c + 1}.mat")[nm][:, 0]
+            assert rel(got, ref["frames"][c, k]) <= 1e-10 or np.abs(ref["frames"][c, k]).max() == 0
+    data = pkg.wavefield.spec2meshgrid_flat_shell(7, inputs, mesh, 16, 16, "velocity", 9, "top", str(out),
+                                                  str(out))
+    saved = loadmat(out / "flat_shell_total_velocities_7_16x16top.mat")["Data"]
+    assert saved.shape == (16, 16, 4) and np.array_equal(saved, data)
+    fields = {c: ref["frames"][:, 5 + k] for k, c in enumerate(("x", "Fix", "y", "Fiy", "z"))}
+    want, _ = R.spec2meshgrid_flat_shell(mesh["nodes"], mesh["coords"], 16, 16, fields, 9, "top",
+                                         float(np.sum(M.CFRP_PLY_T)))
+    assert rel(data, want) <= 1e-10
