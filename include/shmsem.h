@@ -89,6 +89,14 @@ typedef struct {
   int32_t frame_dof;       /* 0 = all DOF components, 1..5: one component (5 = w) */
   int32_t frame_kind;      /* field_variable: 0 velocity, 1 displacement, 2 acceleration,
                               3 all three (main_flat_shell.m:765-885) */
+  /* Pressure loading (main_flat_shell_pressure_excit_c.m:64-82,616-632,705-730): nodal
+   * pressure frames p(node, t_k), linear in time between the frames and 0 outside
+   * (interp1 'linear', 0) at t(nn) = (nn-1)*dt, applied to w as the lumped load
+   * p * sum of w_i w_j detJ over the node's element copies.  All scenarios of a
+   * batch that carry pressure share the frame times. */
+  int32_t n_pframes;       /* 0 = no pressure loading */
+  const double *p_times;   /* [n_pframes] s, increasing */
+  const double *p_nodal;   /* [n_pframes x nnode] row-major (frame after frame), Pa */
 } shm_run;
 
 typedef struct {

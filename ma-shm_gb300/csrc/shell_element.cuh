@@ -70,6 +70,23 @@ __device__ __forceinline__ void store_frame(const FrameSpec& fs, T* __restrict__
   if (sA >= 0) base[sA * npad] = a0 * (uo - T(2) * u + un);
 }
 
+// Pressure loading: nodal frames pf[k][node_pad], lumped area parea[node],
+// per step (row nn-1 of pcoef) the two frames and their weights
+// {f0, f1, c0, c1}; the load on w is parea * (c0 pf[f0] + c1 pf[f1]).
+template <typename T> struct PressureArgs {
+  int npf;                          // 0 = no pressure loading
+  const T* __restrict__ pf;
+  const T* __restrict__ parea;
+  const double* __restrict__ pcoef;
+};
+
+template <typename T>
+__device__ __forceinline__ T pressure_load(const PressureArgs<T>& pr, int nn, int64_t npad, int64_t node) {
+  const double* c = pr.pcoef + 4 * (int64_t)(nn - 1);
+  const T p = (T)c[2] * pr.pf[(int64_t)c[0] * npad + node] + (T)c[3] * pr.pf[(int64_t)c[1] * npad + node];
+  return pr.parea[node] * p;
+}
+
 // Laminate coefficients of one element (composite_plate*.m outputs).
 template <typename T> struct Lam {
   T a11, a12, a16, a22, a26, a66, a44, a45, a55;

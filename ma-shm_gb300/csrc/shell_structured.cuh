@@ -41,6 +41,7 @@ template <typename T> struct StructArgs {
   T* UA;
   T* UB;
   T* outp;  // u_{n+1} destination; null = over u_{n-1}
+  PressureArgs<T> pr;
   const T* __restrict__ minv;
   T k1[5], k2[5];
   const T* __restrict__ mat;
@@ -225,9 +226,10 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
         const int64_t node = pl2.node0 + (int64_t)(5 * ey2 + rr) * pl2.NX + ix;
         const T* bnd = band + gg * BG::GSTRIDE;
         const T mt = a.minv[node], mr = a.minv[a.nnode_pad + node];
+        const T fp = a.pr.npf > 0 ? pressure_load(a.pr, nn, a.nnode_pad, node) : T(0);
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
-          const T F = bnd[(rr * 5 + f) * BG::W + 5 + c];
+          const T F = bnd[(rr * 5 + f) * BG::W + 5 + c] - (f == 4 ? fp : T(0));
           const T u = cur[f * a.nnode_pad + node];
           const T uo = prev[f * a.nnode_pad + node];
           const T im = (f == 1 || f == 3) ? mr : mt;

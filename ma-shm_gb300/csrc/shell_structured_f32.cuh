@@ -69,6 +69,7 @@ struct F32Args {
   float* UA;
   float* UB;
   float* outp;  // u_{n+1} destination; null = over u_{n-1}
+  PressureArgs<float> pr;
   const float* __restrict__ minv;
   float k1[5], k2[5];
   const float2* __restrict__ matp;  // [nmat][20] coefficient pairs
@@ -541,6 +542,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
                   if (f == a.o_field[oi]) F[f] += rv;
               }
           }
+          if (!kAdj && a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, node);
           if (!kAdj && t2.fn > 0) {
             const int iy = 5 * (t2.eyA + r) + j;
             for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)

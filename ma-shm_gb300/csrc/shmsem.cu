@@ -68,6 +68,7 @@ template <typename T> struct GenArgs {
   // frames
   FrameSpec fs;
   T* frames;                      // [nframes][nfields][nnode_pad]
+  PressureArgs<T> pr;
   T a0, a1;
   T blowup;                       // 10*h
   int* flag;
@@ -262,6 +263,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
 #pragma unroll
     for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
   }
+  if (a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, g);
   T* dst = a.outp ? a.outp : prev;
   const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
@@ -395,6 +397,10 @@ struct shm_plan {
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
   float fb_ms[3] = {0.f, 0.f, 0.f};  // last forward_backward: forward, recompute, adjoint (ms)
   int64_t store_cap = -1;             // bytes for states kept by the forward pass (-1 = spare memory)
+  // pressure loading: nodal frames [npf][nnode_pad], lumped areas, per-step weights
+  int npf = 0;
+  void *pf = nullptr, *parea = nullptr;
+  double* pcoef = nullptr;
   int last_nstore = 0;
   double *grad = nullptr, *asig = nullptr;
   int* d_base_adj = nullptr;
@@ -635,6 +641,7 @@ template <typename T> static GenArgs<T> make_args(shm_plan* p) {
   fill_sc(p, a.sc);
   a.fs = p->fspec;
   a.frames = (T*)p->frames;
+  a.pr = PressureArgs<T>{p->npf, (const T*)p->pf, (const T*)p->parea, p->pcoef};
   a.a0 = (T)p->a0;
   a.a1 = (T)p->a1;
   a.blowup = (T)p->blowup;
@@ -986,6 +993,7 @@ static F32Args struct_f32_args(shm_plan* p) {
   fill_sc(p, a.sc);
   a.fs = p->fspec;
   a.frames = (float*)p->frames;
+  a.pr = PressureArgs<float>{p->npf, (const float*)p->pf, (const float*)p->parea, p->pcoef};
   a.a0 = (float)p->a0;
   a.a1 = (float)p->a1;
   a.blowup = (float)p->blowup;
@@ -1054,6 +1062,7 @@ static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
   fill_sc(p, a.sc);
   a.fs = p->fspec;
   a.frames = (T*)p->frames;
+  a.pr = PressureArgs<T>{p->npf, (const T*)p->pf, (const T*)p->parea, p->pcoef};
   a.a0 = (T)p->a0;
   a.a1 = (T)p->a1;
   a.blowup = (T)p->blowup;
@@ -1069,6 +1078,62 @@ static cudaError_t launch_struct_step(shm_plan* p, int kstep, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // plan creation
 // ---------------------------------------------------------------------------
+
+// Pressure loading (main_flat_shell_pressure_excit_c.m:64-82,616-632): nodal
+// frames and areas on the device, and per step nn = 1..nft the interp1
+// ('linear', extrapolation 0) weights of the two frames around t = (nn-1) dt.
+template <typename T>
+static shm_status pressure_build(shm_plan* p, int nscen, const shm_mesh* meshes, const shm_run* runs,
+                                 const std::vector<double>& area) {
+  int npf = 0;
+  const double* times = nullptr;
+  for (int s = 0; s < nscen; ++s) {
+    const shm_run& r = runs[s];
+    if (r.n_pframes <= 0) continue;
+    if (!r.p_times || !r.p_nodal) return bad(p, "run: pressure frames without times or values");
+    if (npf == 0) {
+      npf = r.n_pframes;
+      times = r.p_times;
+      for (int k = 1; k < npf; ++k)
+        if (!(times[k] > times[k - 1])) return bad(p, "run: pressure frame times must increase");
+    } else if (r.n_pframes != npf || !std::equal(times, times + npf, r.p_times)) {
+      return bad(p, "run: scenarios with pressure loading must share the frame times");
+    }
+  }
+  p->npf = npf;
+  if (npf == 0) return SHM_OK;
+  std::vector<T> pf((size_t)npf * p->nnode_pad, T(0)), pa(area.size());
+  for (size_t g = 0; g < area.size(); ++g) pa[g] = (T)area[g];
+  for (int s = 0; s < nscen; ++s) {
+    const shm_run& r = runs[s];
+    if (r.n_pframes <= 0) continue;
+    const int64_t n0 = p->node_off[s], nn_s = meshes[s].nnode;
+    for (int k = 0; k < npf; ++k)
+      for (int64_t g = 0; g < nn_s; ++g) pf[(size_t)k * p->nnode_pad + n0 + g] = (T)r.p_nodal[(size_t)k * nn_s + g];
+  }
+  std::vector<double> coef((size_t)4 * p->nft, 0.0);
+  for (int nn = 1; nn <= p->nft; ++nn) {
+    const double t = (nn - 1) * p->dt;
+    double* c = &coef[(size_t)4 * (nn - 1)];
+    if (t < times[0] || t > times[npf - 1]) continue;  // zero outside the frames
+    int k = 0;
+    while (k + 1 < npf - 1 && t > times[k + 1]) ++k;
+    const int k1 = npf > 1 ? k + 1 : k;
+    const double al = npf > 1 ? (t - times[k]) / (times[k1] - times[k]) : 0.0;
+    c[0] = k;
+    c[1] = k1;
+    c[2] = 1.0 - al;
+    c[3] = al;
+  }
+  T *dpf = nullptr, *dpa = nullptr;
+  shm_status st;
+  if ((st = upload(p, &dpf, pf)) != SHM_OK) return st;
+  if ((st = upload(p, &dpa, pa)) != SHM_OK) return st;
+  if ((st = upload(p, &p->pcoef, coef)) != SHM_OK) return st;
+  p->pf = dpf;
+  p->parea = dpa;
+  return SHM_OK;
+}
 
 template <typename T>
 static shm_status build_device(shm_plan* p, const std::vector<int>& conn, const std::vector<double>& geo,
@@ -1333,10 +1398,10 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
     if (fillc[g] != node_cnt[g]) return bad(p, "mesh: basket maps do not cover every element node");
 
   // diagonal mass (main_flat_shell.m:493-501), summed in basket order
-  std::vector<double> minv((size_t)2 * p->nnode_pad, 0.0);
+  std::vector<double> minv((size_t)2 * p->nnode_pad, 0.0), area((size_t)p->nnode_pad, 0.0);
   p->mass.assign((size_t)5 * p->nnode, 0.0);
   for (int64_t g = 0; g < p->nnode; ++g) {
-    double mt_ = 0, mr_ = 0;
+    double mt_ = 0, mr_ = 0, ar = 0;
     for (int q = row_ptr[g]; q < row_ptr[g + 1]; ++q) {
       const int64_t sl = slots[q];
       if (sl >= P36) continue;
@@ -1344,7 +1409,9 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
       const double W = geo[4 * NPE * FP + c * FP + e];
       mt_ += W * elem_m11[e];
       mr_ += W * elem_I11[e];
+      ar += W;
     }
+    area[g] = ar;
     minv[g] = mt_ > 0 ? 1.0 / mt_ : 0.0;
     minv[p->nnode_pad + g] = mr_ > 0 ? 1.0 / mr_ : 0.0;
     p->mass[5 * g + 0] = mt_;
@@ -1408,6 +1475,9 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
   if ((st = dalloc(p, &p->flag, 4)) != SHM_OK) return st;
   if ((st = dalloc(p, &p->d_base, 4)) != SHM_OK) return st;
   if ((st = set_func_attrs(p)) != SHM_OK) return st;
+  if ((st = (p->prec == 64 ? pressure_build<double>(p, nscen, meshes, runs, area)
+                           : pressure_build<float>(p, nscen, meshes, runs, area))) != SHM_OK)
+    return st;
 
   // path selection
   p->path = 1;
@@ -1949,6 +2019,7 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   a.asig = p->asig;
   a.grad = p->grad;
   a.fs.frm_int = 0;
+  a.pr.npf = 0;  // forward-only loads do not enter the adjoint
   a.nout = 0;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t smem = adj_smem_bytes(sizeof(T) == 8 ? 64 : 32);
@@ -1963,6 +2034,7 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     af.d_base = p->d_base_adj;
     af.nout = 0;
     af.fs.frm_int = 0;
+    af.pr.npf = 0;
     af.asig = p->asig;
     af.grad = p->grad;
   }
@@ -2208,6 +2280,11 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
     p->k2[f] = 1.0 / den;
   }
   if (set_frames(p, r0, 3) != SHM_OK) return SHM_ERR_BAD_ARG;
+  for (int s2 = 0; s2 < nscen; ++s2)
+    if (runs[s2].n_pframes > 0) {
+      p->err = "pressure loading is built for flat-shell plans";
+      return SHM_ERR_UNSUPPORTED;
+    }
   p->blowup = INFINITY;
   p->node_off.assign(nscen + 1, 0);
   p->elem_off.assign(nscen + 1, 0);

@@ -40,7 +40,8 @@ class ShmRun(C.Structure):
                 ("n_sens", C.c_int32), ("sens_ptr", I32P), ("sens_el", I32P),
                 ("pzt_thickness", C.c_double), ("g33", C.c_double), ("e31", C.c_double),
                 ("e32", C.c_double), ("h", C.c_double),
-                ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("frame_kind", C.c_int32)]
+                ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("frame_kind", C.c_int32),
+                ("n_pframes", C.c_int32), ("p_times", F64P), ("p_nodal", F64P)]
 
 
 class ShmSolidMesh(C.Structure):

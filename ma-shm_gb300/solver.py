@@ -35,6 +35,7 @@ class Scenario:
     sensors: list = field(default_factory=list)   # list of 0-based element arrays (PZT sensors)
     pzt: dict | None = None          # pzt_thickness, g33, e31, e32
     signal: np.ndarray | None = None  # st [nft]
+    pressure: dict | None = None     # times [npf] (s), nodal [npf, nnode] (Pa): pressure loading
 
 
 @dataclass
@@ -180,6 +181,12 @@ class Plan:
             r.n_sens = 0
         r.h = run.h
         r.frm_int, r.frame_dof, r.frame_kind = run.frm_int, run.frame_dof, run.frame_kind
+        if sc.pressure is not None:
+            pt = self._arr(sc.pressure["times"], np.float64)
+            pn = self._arr(np.asarray(sc.pressure["nodal"], float).reshape(len(pt), -1), np.float64)
+            r.n_pframes, r.p_times, r.p_nodal = len(pt), native.ptr(pt), native.ptr(pn)
+        else:
+            r.n_pframes = 0
 
     # ------------------------------------------------------------------
     def _check(self, st):

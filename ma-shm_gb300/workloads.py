@@ -240,3 +240,52 @@ def solid_plate(nex=120, L=0.5, T=0.5e-3, f=50e3, seed=0, n_out=8, radius=0.15, 
     sc.delam = info
     run = RunConfig(dt=dt, nft=nft, nn_first=2, eta_xy=ETA_XY, eta_z=ETA_Z, h=float(ply_t.sum()))
     return [sc], run
+
+
+def pressure_from_grid(data: np.ndarray, coords: np.ndarray, Lx: float = 0.5, Ly: float = 0.5) -> np.ndarray:
+    """Nodal pressure frames [nframes, nnode] from gridded frames ``data``
+    [ny, nx, nframes] spanning [0, Lx] x [0, Ly] (the Data array that
+    main_flat_shell_pressure_excit_c.m:65-82 loads; its first index runs
+    along y).  The reference interpolates with MATLAB's scatteredInterpolant
+    (linear on a Delaunay triangulation of the grid, whose diagonal choice on a
+    regular grid is arbitrary); this uses bilinear interpolation, which equals
+    it wherever the field is linear inside a cell."""
+    data = np.asarray(data, float)
+    ny, nx, nf = data.shape
+    fx = np.clip(coords[:, 0] / Lx * (nx - 1), 0, nx - 1)
+    fy = np.clip(coords[:, 1] / Ly * (ny - 1), 0, ny - 1)
+    i0 = np.minimum(fx.astype(int), nx - 2)
+    j0 = np.minimum(fy.astype(int), ny - 2)
+    ax, ay = fx - i0, fy - j0
+    out = np.empty((nf, coords.shape[0]))
+    for k in range(nf):
+        d = data[:, :, k]
+        out[k] = ((1 - ax) * (1 - ay) * d[j0, i0] + ax * (1 - ay) * d[j0, i0 + 1] +
+                  (1 - ax) * ay * d[j0 + 1, i0] + ax * ay * d[j0 + 1, i0 + 1])
+    return out
+
+
+def plate_pressure(nex=10, ney=10, L=0.1, nft=400, f=200e3, npf=25, p0=1e3, seed=0):
+    """Plate loaded by a moving Gaussian pressure spot (a synthetic stand-in for
+    the COMSOL pressure field of main_flat_shell_pressure_excit_c.m), frames on
+    a 41x41 grid every few time steps, dt and the loop as the _c variants
+    (dt = tt/(nft-1), nn = 1..nft)."""
+    lam = M.cfrp_laminate()
+    mesh = MS.structured_plate(L, L, nex, ney)
+    dt = _dt_for(L / nex, L / ney, [lam])
+    tt = dt * (nft - 1)
+    g = np.linspace(0.0, L, 41)
+    X, Y = np.meshgrid(g, g)
+    times = np.linspace(0.0, 0.8 * tt, npf)
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(0.3, 0.7, 2) * L
+    data = np.empty((41, 41, npf))
+    for k, t in enumerate(times):
+        w = np.sin(2 * np.pi * f * t) * np.exp(-((X - x0 - 0.2 * L * t / tt) ** 2 + (Y - y0) ** 2) / (0.05 * L) ** 2)
+        data[:, :, k] = p0 * w
+    nodal = pressure_from_grid(data, mesh["coords"], L, L)
+    outs = MS.circle_sensor_nodes(mesh, L / 2, L / 2, 0.3 * L, 6)
+    sc = Scenario(mesh=mesh, mat_table=M.table_row(lam)[None, :], out_dof=(5 * outs).astype(np.int32),
+                  signal=np.zeros(nft), pressure=dict(times=times, nodal=nodal))
+    run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return [sc], run

@@ -41,7 +41,8 @@ class OracleArgs(C.Structure):
                 ("frm_int", C.c_int32), ("frame_dof", C.c_int32), ("frame_kind", C.c_int32),
                 ("nframes_max", C.c_int32),
                 ("frames", F64P), ("t_frames_step", F64P), ("nthreads", C.c_int32),
-                ("U", F64P), ("uold", F64P), ("frames_written", C.c_int32), ("diverged_at", C.c_int32)]
+                ("U", F64P), ("uold", F64P), ("frames_written", C.c_int32), ("diverged_at", C.c_int32),
+                ("n_pf", C.c_int32), ("p_t1", F64P), ("p_nodal", F64P), ("p_dt", C.c_double)]
 
 
 def build(force: bool = False) -> str:
@@ -161,7 +162,7 @@ class OracleProblem:
 
     def run(self, dt, nft, st, nn_first=2, eta_xy=0.0, eta_z=0.0, force_dof=(), force_val=(), out_dof=(),
             sensors=(), pzt=None, h=0.0, frm_int=0, frame_dof=5, frame_kind=0, U0=None, uold0=None, nthreads=0,
-            nn_last=None):
+            nn_last=None, pressure=None):
         keep = []
         A = self._args(keep)
         a0, a1, mgs, mg2, mg0, cg = self.coefficients(dt, eta_xy, eta_z)
@@ -198,6 +199,13 @@ class OracleProblem:
         A.frm_int, A.frame_dof, A.frame_kind, A.nframes_max = frm_int, frame_dof, frame_kind, nfr
         A.frames, A.t_frames_step = _p(frames), _p(tfs)
         A.nthreads = nthreads
+        if pressure is not None:  # dict(times=[npf], nodal=[npf, nnode]); t_sem = (nn-1)*dt
+            pt1 = np.ascontiguousarray(pressure["times"], float)
+            pnod = np.ascontiguousarray(pressure["nodal"], float).reshape(len(pt1), self.nnode)
+            keep += [pt1, pnod]
+            A.n_pf, A.p_t1, A.p_nodal, A.p_dt = len(pt1), _p(pt1), _p(pnod), dt
+        else:
+            A.n_pf = 0
         U = np.zeros(self.ndof) if U0 is None else np.ascontiguousarray(U0, float).copy()
         Uo = np.zeros(self.ndof) if uold0 is None else np.ascontiguousarray(uold0, float).copy()
         A.U, A.uold = _p(U), _p(Uo)

@@ -87,6 +87,12 @@ typedef struct {
   /* result */
   int32_t frames_written;
   int32_t diverged_at; /* 0 if fine, else nn */
+  /* pressure loading (main_flat_shell_pressure_excit_c.m:64-82,616-632,
+     705-730): nodal frames p_nodal[k*nnode + node] at times p_t1[k];
+     t_sem = (nn-1)*p_dt; 0 = none */
+  int32_t n_pf;
+  const double *p_t1, *p_nodal;
+  double p_dt;
 } oracle_args;
 
 static inline void spmv_block(int nnz, const int32_t *row, const int32_t *col, const double *val,
@@ -114,6 +120,13 @@ int oracle_flat_shell_run(oracle_args *A) {
   double *F = (double *)calloc((size_t)ndof, sizeof(double));
   double *unew = (double *)calloc((size_t)ndof, sizeof(double));
   double *Vsum = (double *)calloc((size_t)(fen > 0 ? fen : 1), sizeof(double));
+  double *Fpl = NULL, *Fpr = NULL, *pt = NULL;
+  if (A->n_pf > 0) {
+    Fpl = (double *)calloc((size_t)5 * L, sizeof(double));
+    Fpr = (double *)calloc((size_t)ndof, sizeof(double));
+    pt = (double *)calloc((size_t)A->nnode, sizeof(double));
+    if (!Fpl || !Fpr || !pt) return -1;
+  }
   if (!F2 || !F || !unew || !Vsum) return -1;
   double *U = A->U, *uold = A->uold;
   int frame_c = 0;
@@ -252,11 +265,43 @@ int oracle_flat_shell_run(oracle_args *A) {
       for (int r = 0; r < A->rows5; ++r)
         if (g[r] > 0) F[g[r] - 1] = F[g[r] - 1] + F2[l[r] - 1];
     }
-    /* time integration, main_flat_shell.m:742-750 */
+    /* pressure: pt = interp1(t1, p', t_sem, 'linear', 0); Fi(5:5:end) = pt';
+       fl = Fi(Iw).*WWDetJ; Fp(5:5:end) = fl; baskets into F_pressure */
+    if (A->n_pf > 0) {
+      const double ts = (nn - 1) * A->p_dt;
+      const int np = A->n_pf;
+      int k = -1;
+      if (ts >= A->p_t1[0] && ts <= A->p_t1[np - 1]) {
+        k = 0;
+        while (k + 1 < np - 1 && ts > A->p_t1[k + 1]) ++k;
+      }
+      for (int q = 0; q < A->nnode; ++q) {
+        if (k < 0) {
+          pt[q] = 0.0;
+        } else if (np == 1) {
+          pt[q] = A->p_nodal[q];
+        } else {
+          const double y0 = A->p_nodal[(size_t)k * A->nnode + q], y1 = A->p_nodal[(size_t)(k + 1) * A->nnode + q];
+          pt[q] = y0 + (y1 - y0) * ((ts - A->p_t1[k]) / (A->p_t1[k + 1] - A->p_t1[k]));
+        }
+      }
+      for (int l = 0; l < L; ++l) Fpl[5 * (size_t)l + 4] = pt[A->nodes[l] - 1] * A->WWDetJ[l];
+      memset(Fpr, 0, sizeof(double) * ndof);
+      for (int b = 0; b < 12; ++b) {
+        const int64_t *g = A->IGd + (size_t)b * A->rows5;
+        const int64_t *l = A->ILd + (size_t)b * A->rows5;
+        for (int r = 0; r < A->rows5; ++r)
+          if (g[r] > 0) Fpr[g[r] - 1] = Fpr[g[r] - 1] + Fpl[l[r] - 1];
+      }
+    }
+    /* time integration, main_flat_shell.m:742-750 (+ F_pressure,
+       main_flat_shell_pressure_excit_c.m:730) */
     const double s_nn = A->st[nn - 1];
 #pragma omp parallel for schedule(static)
     for (int d = 0; d < ndof; ++d) {
-      double f = -F[d] + A->mg2[d] * U[d] + A->Fa[d] * s_nn - A->mg[d] * uold[d] + A->a1 * A->cg[d] * uold[d];
+      double f = -F[d] + A->mg2[d] * U[d] + A->Fa[d] * s_nn;
+      if (Fpr) f = f + Fpr[d];
+      f = f - A->mg[d] * uold[d] + A->a1 * A->cg[d] * uold[d];
       unew[d] = A->mg0[d] * f;
     }
     /* outputs: displacement before the update (:752-764) */
@@ -303,6 +348,9 @@ int oracle_flat_shell_run(oracle_args *A) {
   free(F);
   free(unew);
   free(Vsum);
+  free(Fpl);
+  free(Fpr);
+  free(pt);
   return 0;
 }
 

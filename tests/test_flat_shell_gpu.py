@@ -26,7 +26,7 @@ def oracle_run(sc, run, **kw):
     return orc, orc.run(run.dt, run.nft, sc.signal, nn_first=run.nn_first, eta_xy=run.eta_xy, eta_z=run.eta_z,
                         force_dof=sc.force_dof, force_val=sc.force_val, out_dof=sc.out_dof, sensors=sens,
                         pzt=sc.pzt, h=run.h, frm_int=run.frm_int, frame_dof=run.frame_dof,
-                        frame_kind=run.frame_kind, **kw)
+                        frame_kind=run.frame_kind, pressure=sc.pressure, **kw)
 
 
 def small_case(pkg, nex=5, ney=4, T=4e-5, nft_cap=400, frames=0, sensors=False, keep=False):
@@ -305,3 +305,17 @@ def test_delaminated_plate_matches_oracle(pkg, precision):
         g2 = p2.forward()[0]
         p2.close()
         assert rel(got["displ"], g2["displ"]) > 1e-2
+
+
+@pytest.mark.parametrize("precision,path", [(64, 1), (64, 2), (32, 1), (32, 2)])
+def test_pressure_loaded_plate_matches_oracle(pkg, precision, path):
+    """Moving pressure spot (nodal frames, linear in time, zero after the last
+    frame) on the general and the structured kernels."""
+    scs, run = pkg.workloads.plate_pressure(nex=10, ney=10, L=0.1, nft=400)
+    plan = pkg.Plan(scs, run, precision=precision, path=path)
+    assert plan.info["path"] == path
+    got = plan.forward()[0]
+    plan.close()
+    _, ref = oracle_run(scs[0], run)
+    assert np.abs(ref["displ"]).max() > 0
+    assert rel(got["displ"], ref["displ"]) <= (FP64_TOL if precision == 64 else FP32_TOL)
