@@ -103,6 +103,19 @@ def add_piezo_layer(lam: dict, Qpzt: np.ndarray, rho_pzt: float, t_pzt: float) -
     """Surface-bonded PZT layer between z = h/2 and h/2 + t/2 added to a laminate
     row, the reference's treatment (composite_plate_c_delam_pzt.m:186-215,
     including its lever arm t/2 and shear thickness h + t)."""
+    return add_surface_layer(lam, Qpzt, rho_pzt, t_pzt)
+
+
+def add_added_mass(lam: dict, Qm: np.ndarray, rho_m: float, t_m: float) -> dict:
+    """Added mass bonded to the top surface (composite_plate_c_added_mass_pzt.m:195-240):
+    the same surface-layer integrals as the PZT layer with the mass's own
+    stiffness Qm (6x6, Voigt x y z yz xz xy), density and thickness."""
+    return add_surface_layer(lam, Qm, rho_m, t_m)
+
+
+def add_surface_layer(lam: dict, Qpzt: np.ndarray, rho_pzt: float, t_pzt: float) -> dict:
+    """Layer between z = h/2 and h/2 + t/2 on a laminate row (lever arm t/2,
+    shear-correction thickness h + t, as the reference's surface layers)."""
     h = lam["h"]
     o = dict(lam)
     z1, z2 = h / 2, h / 2 + t_pzt / 2

@@ -187,3 +187,21 @@ def test_solid_mesh_and_delamination_split(pkg):
     lower = d["nodes"][0:16, 72:]
     assert len(np.intersect1d(upper, lower)) == len(np.unique(lower)) - 81
     np.testing.assert_allclose(d["coords"][-81:], m["coords"][d["split_nodes"] - 1])
+
+
+def test_added_mass_layer_matches_oracle_surface_layer(pkg):
+    """composite_plate_c_added_mass_pzt.m adds the mass with the PZT layer's
+    integrals (:195-240); the oracle's add_pzt_layer restates them."""
+    M = pkg.materials
+    q = M.ply_stiffness(**M.CFRP_PLY)
+    lam = M.laminate(q, M.CFRP_RHO, M.CFRP_PLY_T, M.CFRP_ANGLES)
+    Qm = np.zeros((6, 6))
+    E, nu = 70e9, 0.33
+    Qm[0, 0] = Qm[1, 1] = E / (1 - nu ** 2)
+    Qm[0, 1] = Qm[1, 0] = nu * E / (1 - nu ** 2)
+    Qm[3, 3] = Qm[4, 4] = Qm[5, 5] = E / (2 * (1 + nu))
+    got = M.add_added_mass(lam, Qm, 2700.0, 1e-3)
+    ref = R.add_pzt_layer(dict(lam), lam["h"], 2700.0, 1e-3, Qm)
+    for k in M.ABD_KEYS:
+        assert np.isclose(got[k], ref[k], rtol=1e-13, atol=1e-13 * abs(ref[k]) + 1e-300), k
+    assert got["m11"] > lam["m11"] and got["d11"] > lam["d11"]
