@@ -366,6 +366,13 @@ def hanning_signal(dt, nft, f_1, f_2, t_1=0.0):
     return t, st
 
 
+def random_signal(nft: int, seed: int = 0) -> np.ndarray:
+    """White-noise excitation st ~ N(0, 1) of length nft
+    (main_flat_shell_multi_pzt_c_random_exc_signals.m:137-139 draws it with
+    MATLAB's randn; the stream here is numpy's, seeded)."""
+    return np.random.default_rng(seed).standard_normal(nft)
+
+
 def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", output_name: str = ".",
                     tasks=(), precision: int = 64, variant: str = "main_flat_shell"):
     """Flat-shell forward solve with the reference's interface and outputs.

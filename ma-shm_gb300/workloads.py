@@ -289,3 +289,36 @@ def plate_pressure(nex=10, ney=10, L=0.1, nft=400, f=200e3, npf=25, p0=1e3, seed
                   signal=np.zeros(nft), pressure=dict(times=times, nodal=nodal))
     run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
     return [sc], run
+
+
+def plate_multi_pzt(nex=40, L=0.2, n_pzt=3, actuator_no=2, d_pzt=10e-3, t_pzt=0.2e-3, V0=100.0, nft=600,
+                    f=150e3, random=False, seed=0):
+    """main_flat_shell_multi_pzt_c.m: n_pzt PZT discs on a circle, all bonded
+    (PZT layer in their elements) and all sensors; disc ``actuator_no``
+    (1-based) is driven (:150-230).  ``random`` drives it with white noise
+    (main_flat_shell_multi_pzt_c_random_exc_signals.m:137-139) instead of the
+    Hann burst."""
+    from . import pzt as PZ
+    from .solver import random_signal
+    lam = M.cfrp_laminate()
+    mesh = MS.structured_plate(L, L, nex, nex)
+    p = M.pzt5a()
+    pm = M.pzt_material(p["S"], p["d"], p["epsT"], 0.0)
+    lam_p = M.add_piezo_layer(lam, pm["Qpzt"], p["rho"], t_pzt)
+    ang = 2 * np.pi * np.arange(n_pzt) / n_pzt
+    discs = [MS.elements_in_disc(mesh, L / 2 + 0.25 * L * np.cos(a), L / 2 + 0.25 * L * np.sin(a), d_pzt / 2)
+             for a in ang]
+    elem_mat = np.zeros(nex * nex, np.int32)
+    for d in discs:
+        elem_mat[d] = 1
+    Fa = PZ.actuator_loads(mesh, discs[actuator_no - 1], t_pzt, lam["h"], V0, pm["epzt"], pm["gpzt"])
+    nzi = np.nonzero(Fa)[0]
+    dt = _dt_for(L / nex, L / nex, [lam, lam_p])
+    st = random_signal(nft, seed) if random else hanning_signal(dt, nft, f / 5, f, 0.0)[1]
+    centre = MS.nearest_node(mesh["coords"], L / 2, L / 2)
+    sc = Scenario(mesh=mesh, mat_table=np.stack([M.table_row(lam), M.table_row(lam_p)]), elem_mat=elem_mat,
+                  force_dof=(nzi + 1).astype(np.int32), force_val=Fa[nzi],
+                  out_dof=np.array([5 * centre], np.int32), signal=st, sensors=discs,
+                  pzt=dict(pzt_thickness=t_pzt, g33=pm["g33"], e31=pm["e31"], e32=pm["e32"]))
+    run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=ETA_XY, eta_z=ETA_Z, h=lam["h"])
+    return [sc], run

@@ -319,3 +319,23 @@ def test_pressure_loaded_plate_matches_oracle(pkg, precision, path):
     _, ref = oracle_run(scs[0], run)
     assert np.abs(ref["displ"]).max() > 0
     assert rel(got["displ"], ref["displ"]) <= (FP64_TOL if precision == 64 else FP32_TOL)
+
+
+@pytest.mark.parametrize("precision,path,random", [(64, 1, False), (64, 2, True), (32, 2, False)])
+def test_multi_pzt_actuator_and_sensors_match_oracle(pkg, precision, path, random):
+    """main_flat_shell_multi_pzt_c.m: three bonded PZTs, the second driven
+    (Hann burst or white noise), every PZT's voltage recorded."""
+    scs, run = pkg.workloads.plate_multi_pzt(nex=16, L=0.08, nft=200, random=random)
+    plan = pkg.Plan(scs, run, precision=precision, path=path)
+    assert plan.info["path"] == path
+    got = plan.forward()[0]
+    plan.close()
+    _, ref = oracle_run(scs[0], run)
+    assert got["voltage"].shape == ref["voltage"].shape == (run.nft, 3)
+    assert np.all(np.abs(ref["voltage"]).max(axis=0) > 0)
+    if precision == 64:
+        assert rel(got["voltage"], ref["voltage"]) <= FP64_TOL
+        assert rel(got["displ"], ref["displ"]) <= FP64_TOL
+    else:
+        assert rel(got["voltage"], ref["voltage"]) <= FP32_VOLT_TOL
+        assert rel(got["displ"], ref["displ"]) <= FP32_TOL
