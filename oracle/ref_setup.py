@@ -897,3 +897,125 @@ def spec2meshgrid_flat_shell(nodes1, coords, Nx, Ny, fields, motion, shell_surfa
         ZI = np.einsum("kp,kp->p", N, ZA)
         Data[:, :, f] = ZI.reshape((Nx, Ny), order="F")
     return Data, dict(xp=xp, yp=yp, owner=owner, ksi_p=ksi_p, eta_p=eta_p, max_err=max_err)
+
+
+# --------------------------------------------------------------------------
+# quad mesh to spectral elements
+# --------------------------------------------------------------------------
+
+
+def change_turn_quad(nodes, pqs):
+    """``src/models/flat_shell/mesher/change_turn_quad.m``: 2x2 Lagrange
+    derivatives at the corners (tensor order m = [1,2,4,3]); an element with a
+    non-positive Jacobian determinant is renumbered m3 = [1,4,3,2]."""
+    nodes = np.array(nodes, dtype=np.int64)
+    n = 2
+    m = [0, 1, 3, 2]
+    m3 = [0, 3, 2, 1]
+    ksi = np.array([-1.0, 1.0])
+    V = np.array([[ksi[j] ** i for j in range(n)] for i in range(n)])
+    Q = np.linalg.inv(V)
+    Vx = np.zeros((n, n))
+    for k in range(n):
+        for i in range(n):
+            for j in range(1, n):
+                Vx[k, i] += Q[i, j] * j * ksi[k] ** (j - 1)
+    for ne in range(nodes.shape[0]):
+        x = [pqs[nodes[ne, m[c]] - 1, 0] for c in range(4)]
+        y = [pqs[nodes[ne, m[c]] - 1, 1] for c in range(4)]
+        bad = False
+        for j in range(n):
+            for i in range(n):
+                J11 = sum(Vx[i, kx] * x[j * n + kx] for kx in range(n))
+                J12 = sum(Vx[i, kx] * y[j * n + kx] for kx in range(n))
+                J22 = sum(Vx[j, ky] * y[ky * n + i] for ky in range(n))
+                J21 = sum(Vx[j, ky] * x[ky * n + i] for ky in range(n))
+                if J11 * J22 - J12 * J21 <= 0:
+                    bad = True
+        if bad:
+            nodes[ne] = nodes[ne, m3]
+    return nodes
+
+
+def quad2spectral_fiborek(elementNodes_fem, nodeCoordinates_fem, N):
+    """``src/models/flat_shell/mesher/quad2spectral_Fiborek.m``, step by step:
+    rounded edge midpoints (``edgegeometry``), edge-interior nodes numbered by
+    ``unique(...,'rows')``, interior nodes as intersections of the lines between
+    opposite edge nodes (Cramer's rule of the sparse block products, taken in
+    the column-major order of ``W(AA)``), the row assembly ``elementNodes_pl3``
+    and the boundary nodes of edges whose midpoint occurs once.  1-based."""
+    efem = np.asarray(elementNodes_fem, dtype=np.int64)
+    pos = np.asarray(nodeCoordinates_fem, dtype=float)
+    n = N + 1
+    fen = efem.shape[0]
+    n_int = n - 2
+    ksi, _ = gll(n)
+    ksi_int = ksi[1:n - 1]
+
+    def mround(v):
+        return np.sign(v) * np.floor(np.abs(v) + 0.5)
+
+    def edgegeometry(dim):
+        nC = pos[efem[:, [0, 1, 2, 3, 0]] - 1, dim]                 # [fen, 5]
+        mid = (nC[:, 1:5] + nC[:, 0:4]) / 2
+        mid = mround(mid.reshape(-1) * 1e6) * 1e-6                   # reshape(mid',[],1)
+        ln = ((nC[:, 1:5] - nC[:, 0:4]) / 2).reshape(-1)
+        return mid, ln
+
+    mids, lens, temps = [], [], []
+    for dim in range(3):
+        mid, ln = edgegeometry(dim)
+        mids.append(mid)
+        lens.append(ln)
+        temps.append((mid[:, None] + ln[:, None] * ksi_int[None, :]).reshape(-1))   # reshape(tmp',[],1)
+    ic = np.stack(temps, axis=1)
+    b1, n1 = np.unique(ic, axis=0, return_inverse=True)          # unique(...,'first','rows')
+    n1 = n1.reshape(-1) + 1
+    nce = b1
+    en_edge = n1.reshape(fen, 4 * n_int)
+    maxe = int(en_edge.max())
+    en_int = (np.arange(1, fen * n_int ** 2 + 1) + maxe).reshape(fen, n_int ** 2)
+    cols = lambda lo, hi, step=1: np.arange(lo, hi + (1 if step > 0 else -1), step) - 1
+    n_el1 = en_edge[:, cols(1, n_int)]
+    n_el2 = en_edge[:, cols(1 + n_int, 2 * n_int)]
+    n_el3 = en_edge[:, cols(3 * n_int, 1 + 2 * n_int, -1)]
+    n_el4 = en_edge[:, cols(4 * n_int, 1 + 3 * n_int, -1)]
+    X_int, Y_int = [], []
+    for e in range(fen):
+        x1, y1 = nce[n_el1[e] - 1, 0], nce[n_el1[e] - 1, 1]
+        x3, y3 = nce[n_el3[e] - 1, 0], nce[n_el3[e] - 1, 1]
+        x2, y2 = nce[n_el2[e] - 1, 0], nce[n_el2[e] - 1, 1]
+        x4, y4 = nce[n_el4[e] - 1, 0], nce[n_el4[e] - 1, 1]
+        A13, B13, C13 = y3 - y1, x1 - x3, (y1 - y3) * x1 + (x3 - x1) * y1
+        A42, B42, C42 = y2 - y4, x4 - x2, (y4 - y2) * x4 + (x2 - x4) * y4
+        for mm in range(n_int):          # column of the block (42 index)
+            for kk in range(n_int):      # row of the block (13 index)
+                W = A13[kk] * B42[mm] - B13[kk] * A42[mm]
+                X_int.append((B13[kk] * C42[mm] - C13[kk] * B42[mm]) / W)
+                Y_int.append((C13[kk] * A42[mm] - A13[kk] * C42[mm]) / W)
+    zs = np.unique(nce[:, 2])
+    nci = np.stack([np.array(X_int), np.array(Y_int), np.full(len(X_int), zs[0])], axis=1)
+    en_int_all = np.concatenate([en_edge, en_int], axis=1) + int(efem.max())
+    ensem = np.concatenate([efem, en_int_all], axis=1)            # columns 1..4, then 4 + ...
+    spec_coords = np.concatenate([pos, nce, nci])
+    pl3 = np.zeros_like(ensem)
+    for ii in range(1, n + 1):
+        if ii == 1:
+            c = [1] + list(range(4 + 1, 4 + n_int + 1)) + [2]
+        elif ii < n:
+            c = ([4 + 4 * n_int - ii + 2] + list(range((ii - 2) * n_int + 1 + 4 + 4 * n_int,
+                                                       (ii - 2) * n_int + 4 + 4 * n_int + n_int + 1))
+                 + [ii - 1 + 4 + 1 * n_int])
+        else:
+            c = [4] + list(range(4 + 3 * n_int, 4 + 2 * n_int, -1)) + [3]
+        pl3[:, n * (ii - 1):n * ii] = ensem[:, np.array(c) - 1]
+    mid3 = np.stack(mids, axis=1)
+    _, n0, cnt = np.unique(mid3, axis=0, return_inverse=True, return_counts=True)
+    n0 = n0.reshape(-1)
+    single = cnt[n0] == 1
+    edges = [list(range(1, n + 1)), list(range(n, n * n + 1, n)), list(range(1 + n * (n - 1), n * n + 1)),
+             list(range(1, 1 + n * (n - 1) + 1, n))]
+    en_edge_cols = pl3[:, np.array(sum(edges, [])) - 1]           # [fen, 4n]
+    mask = np.repeat(single.reshape(fen, 4), n, axis=1)
+    boundary = np.unique(en_edge_cols[mask])
+    return pl3, spec_coords, boundary

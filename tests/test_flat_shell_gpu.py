@@ -339,3 +339,27 @@ def test_multi_pzt_actuator_and_sensors_match_oracle(pkg, precision, path, rando
     else:
         assert rel(got["voltage"], ref["voltage"]) <= FP32_VOLT_TOL
         assert rel(got["displ"], ref["displ"]) <= FP32_TOL
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_unstructured_quad_mesh_matches_oracle(pkg, precision):
+    """gmsh-style jittered quads (one clockwise, turned by change_turn_quad)
+    converted by quad2spectral run on the general path."""
+    from tests.test_mesher import jittered_quads
+    q, pos = jittered_quads(nx=7, ny=6, Lx=0.06, Ly=0.05, amp=0.0025, seed=3, flip=(4,))
+    q = pkg.mesher.change_turn_quad(q, pos)
+    nodes, coords, _ = pkg.mesher.quad2spectral(q, pos, 5)
+    mesh = dict(nodes=nodes, coords=coords, structured=False)
+    lam = pkg.materials.cfrp_laminate()
+    run = pkg.RunConfig(dt=1.5e-8, nft=400, nn_first=2, eta_xy=4e2, eta_z=4e3, h=lam["h"])
+    _, st = pkg.hanning_signal(run.dt, run.nft, 60e3, 300e3)
+    centre = pkg.mesh.nearest_node(coords, 0.03, 0.025)
+    sc = pkg.Scenario(mesh=mesh, mat_table=pkg.materials.table_row(lam)[None, :], force_dof=np.array([5 * centre]),
+                      force_val=np.array([1.0]), out_dof=np.arange(5, 5 * coords.shape[0], 97), signal=st)
+    plan = pkg.Plan([sc], run, precision=precision, path=0)
+    assert plan.info["path"] == 1
+    got = plan.forward()[0]
+    plan.close()
+    _, ref = oracle_run(sc, run)
+    assert np.abs(ref["displ"]).max() > 0
+    assert rel(got["displ"], ref["displ"]) <= (FP64_TOL if precision == 64 else FP32_TOL)
