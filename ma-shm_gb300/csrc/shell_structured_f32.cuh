@@ -147,28 +147,38 @@ __device__ __forceinline__ const GroupTask& pick(const GroupTask* gt, int g) {
   }
 }
 
-// copy node rows [r0, r0+nr) (relative to the task's first node row) of u_n
-// into the ring; columns outside the plate are left untouched (never read)
-template <int EW>
+// copy node rows [r0, r0+NR) (relative to the task's first node row) of u_n
+// into ring slots slot0, slot0+1, ... (mod URING); warp f < 5 copies field f
+// of every lane group; columns outside the plate are left untouched (never read)
+template <int EW, int NR>
 __device__ __forceinline__ void ring_load(float* ring, const float* __restrict__ cur, int64_t nnode_pad,
-                                          const GroupTask* gt, int r0, int nr) {
+                                          const GroupTask* gt, int r0, int slot0) {
   using GM = F32Geom<EW>;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per_group = nr * 5;
-  for (int rf = warp; rf < GM::G * per_group; rf += CTA_THREADS / 32) {
-    const int gg = rf / per_group;
-    const int rem = rf % per_group;
-    const int rr = rem / 5, f = rem % 5;
-    const GroupTask& t = pick<GM::G>(gt, gg);
+  constexpr int G = GM::G, W = GM::W, UR = GM::URING;
+  const int f = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (f >= 5) return;
+#pragma unroll
+  for (int gg = 0; gg < G; ++gg) {
+    const GroupTask& t = pick<G>(gt, gg);
     if (!t.has) continue;
-    const int row = 5 * t.eyA + r0 + rr;
-    if (row > 5 * t.ney) continue;
     const int col0 = 5 * (t.strip * (EW - 1) - 1);
-    float* dst = ring + gg * GM::UGS + (((r0 + rr) % GM::URING) * 5 + f) * GM::W;
-    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row * t.NX + col0;
-    for (int c = lane; c < GM::W; c += 32) {
-      const int col = col0 + c;
-      if (col >= 0 && col < t.NX) cp_async4(dst + c, src + c);
+    const int row0 = 5 * t.eyA + r0;
+    const int NX = t.NX, rmax = 5 * t.ney;
+    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row0 * NX + col0;
+    int sl = slot0;
+#pragma unroll
+    for (int rr = 0; rr < NR; ++rr) {
+      if (row0 + rr <= rmax) {
+        float* dst = ring + gg * GM::UGS + (sl * 5 + f) * W;
+#pragma unroll
+        for (int c0 = 0; c0 < W; c0 += 32) {
+          const int c = c0 + lane;
+          const int col = col0 + c;
+          if (c < W && col >= 0 && col < NX) cp_async4(dst + c, src + c);
+        }
+      }
+      src += NX;
+      if (++sl == UR) sl = 0;
     }
   }
 }
@@ -254,14 +264,15 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     }
 
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
-    ring_load<EW>(ring, cur, a.nnode_pad, gt, 0, 6);
+    ring_load<EW, 6>(ring, cur, a.nnode_pad, gt, 0, 0);
     cp_async_commit();
 
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
     int rb6 = 0;  // r mod 6
     for (int r = 0; r < maxrows; ++r) {
-      // next element row's five new node rows (ring slots free since row r-1)
-      if (r + 1 < maxrows) ring_load<EW>(ring, cur, a.nnode_pad, gt, 5 * r + 6, 5);
+      // next element row's five new node rows (ring slots free since row r-1):
+      // node rows 5r+6 .. 5r+10 go to slots (rb + 6) mod 11 onwards
+      if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6);
       cp_async_commit();
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       __syncthreads();
