@@ -149,10 +149,30 @@ __device__ __forceinline__ const GroupTask& pick(const GroupTask* gt, int g) {
 
 // copy node rows [r0, r0+NR) (relative to the task's first node row) of u_n
 // into ring slots slot0, slot0+1, ... (mod URING); warp f < 5 copies field f
-// of every lane group; columns outside the plate are left untouched (never read)
+// of every lane group; columns outside the plate are left untouched (never
+// read).  colmask bit (gg*8 + chunk) says whether this lane's column
+// chunk*32 + lane of group gg lies on the plate (fixed for a task).
+template <int EW>
+__device__ __forceinline__ unsigned ring_colmask(const GroupTask* gt) {
+  using GM = F32Geom<EW>;
+  const int lane = threadIdx.x & 31;
+  unsigned m = 0;
+#pragma unroll
+  for (int gg = 0; gg < GM::G; ++gg) {
+    const GroupTask& t = pick<GM::G>(gt, gg);
+    const int col0 = 5 * (t.strip * (EW - 1) - 1);
+#pragma unroll
+    for (int ch = 0; ch * 32 < GM::W; ++ch) {
+      const int c = ch * 32 + lane;
+      if (t.has && c < GM::W && (unsigned)(col0 + c) < (unsigned)t.NX) m |= 1u << (gg * 8 + ch);
+    }
+  }
+  return m;
+}
+
 template <int EW, int NR>
 __device__ __forceinline__ void ring_load(float* ring, const float* __restrict__ cur, int64_t nnode_pad,
-                                          const GroupTask* gt, int r0, int slot0) {
+                                          const GroupTask* gt, int r0, int slot0, unsigned colmask) {
   using GM = F32Geom<EW>;
   constexpr int G = GM::G, W = GM::W, UR = GM::URING;
   const int f = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -164,18 +184,19 @@ __device__ __forceinline__ void ring_load(float* ring, const float* __restrict__
     const int col0 = 5 * (t.strip * (EW - 1) - 1);
     const int row0 = 5 * t.eyA + r0;
     const int NX = t.NX, rmax = 5 * t.ney;
-    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row0 * NX + col0;
+    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row0 * NX + col0 + lane;
+    const unsigned dbase =
+        static_cast<unsigned>(__cvta_generic_to_shared(ring + gg * GM::UGS + f * W + lane));
     int sl = slot0;
 #pragma unroll
     for (int rr = 0; rr < NR; ++rr) {
       if (row0 + rr <= rmax) {
-        float* dst = ring + gg * GM::UGS + (sl * 5 + f) * W;
+        const unsigned drow = dbase + (unsigned)(sl * 5 * W) * 4u;
 #pragma unroll
-        for (int c0 = 0; c0 < W; c0 += 32) {
-          const int c = c0 + lane;
-          const int col = col0 + c;
-          if (c < W && col >= 0 && col < NX) cp_async4(dst + c, src + c);
-        }
+        for (int ch = 0; ch * 32 < W; ++ch)
+          if (colmask & (1u << (gg * 8 + ch)))
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(drow + ch * 128u), "l"(src + ch * 32)
+                         : "memory");
       }
       src += NX;
       if (++sl == UR) sl = 0;
@@ -264,7 +285,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     }
 
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
-    ring_load<EW, 6>(ring, cur, a.nnode_pad, gt, 0, 0);
+    const unsigned colmask = ring_colmask<EW>(gt);
+    ring_load<EW, 6>(ring, cur, a.nnode_pad, gt, 0, 0, colmask);
     cp_async_commit();
 
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
@@ -272,7 +294,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     for (int r = 0; r < maxrows; ++r) {
       // next element row's five new node rows (ring slots free since row r-1):
       // node rows 5r+6 .. 5r+10 go to slots (rb + 6) mod 11 onwards
-      if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6);
+      if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
       cp_async_commit();
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       __syncthreads();
