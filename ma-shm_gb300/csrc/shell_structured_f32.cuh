@@ -506,31 +506,37 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       // band accumulation.  Logical row j of this element row is physical row
       // (j - r) mod 6.  Row 0 carries the previous element row's top line and
-      // is added to; rows 1..5 start here, so pass 1 stores columns i = 0..4
-      // (lanes without an element store zeros) and pass 2 adds column i = 5
-      // (the next lane's column 0), or stores it on the strip's last lane.
+      // is added to; rows 1..5 start here and are stored.  Column i = 5 of a
+      // lane's element is column 0 of the next lane's: it moves one lane up
+      // by shuffle (lanes of a group are consecutive), and the strip's last
+      // lane writes it itself.
       int prow = j - rb6;
       if (prow < 0) prow += 6;
       {
         float* dst = fb + prow * 5 * W + 5 * q;
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+          const float from_left = __shfl_up_sync(0xffffffffu, out[f][5], 1);
+          if (q > 0) out[f][0] += from_left;
+        }
         if (j == 0) {
 #pragma unroll
           for (int f = 0; f < 5; ++f)
 #pragma unroll
             for (int i = 0; i < 5; ++i) dst[f * W + i] += out[f][i];
+          if (q == EW - 1) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) dst[f * W + 5] += out[f][5];
+          }
         } else {
 #pragma unroll
           for (int f = 0; f < 5; ++f)
 #pragma unroll
             for (int i = 0; i < 5; ++i) dst[f * W + i] = out[f][i];
-        }
-        __syncthreads();
-        if (j == 0 || q < EW - 1) {
+          if (q == EW - 1) {
 #pragma unroll
-          for (int f = 0; f < 5; ++f) dst[f * W + 5] += out[f][5];
-        } else {
-#pragma unroll
-          for (int f = 0; f < 5; ++f) dst[f * W + 5] = out[f][5];
+            for (int f = 0; f < 5; ++f) dst[f * W + 5] = out[f][5];
+          }
         }
         __syncthreads();
       }
