@@ -30,9 +30,9 @@ sys.path.insert(0, REPO)
 
 ALG_BYTES = {32: 16.0, 64: 32.0}   # algorithmic bytes per DOF-step (u_n, u_n-1, u_n+1, 1/M)
 # DRAM bytes (read + write) per DOF of one k_struct_step_f32 launch, from the ncu
-# capture in profiles/k_struct_step_f32_batch64_v3.md (292.9 + 82.4 MB for the
+# capture in profiles/k_struct_step_f32_batch64_v4.md (292.9 + 83.5 MB for the
 # 64-plate batch of 30 001 270 DOF); traffic grows with the DOF count
-F32_TRAFFIC_PER_DOF = (292.910336e6 + 82.395648e6) / 30001270
+F32_TRAFFIC_PER_DOF = (292.914176e6 + 83.467264e6) / 30001270
 METRIC = "DOF-steps/s (batched flat-shell SEM forward, 512 uneven plates)"
 
 
