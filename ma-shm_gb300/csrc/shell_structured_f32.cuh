@@ -58,7 +58,8 @@ template <int EW> struct F32Geom {
 template <int EW>
 constexpr size_t struct_f32_smem_bytes() {
   using GM = F32Geom<EW>;
-  return sizeof(float) * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS + GM::G * (GM::UGS + GM::FGS));
+  return sizeof(float) * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS + GM::G * (GM::UGS + GM::FGS)) +
+         sizeof(float2) * LAMP * CTA_ELEMS;
 }
 
 struct F32Args {
@@ -221,6 +222,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
   float* ring = vred + NP * CTA_ELEMS;
   float* band = ring + G * GM::UGS;
+  // laminate pairs of the row's elements, [LAMP][lane] (staged by all warps in phase A)
+  float2* lsm = reinterpret_cast<float2*>(band + G * GM::FGS);
 
   const int nn = *a.d_base + kstep;
   const bool odd = ((nn - a.nn_first) & 1);
@@ -304,6 +307,16 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       const long long egrid = eg0 + (long long)r * t_nex;
       auto slot = [rb](int k) { const int s = rb + k; return s >= UR ? s - UR : s; };
 
+      // stage the element's laminate pairs: warp j loads pairs j, j+6, ...
+      if (valid) {
+        const float2* mp = a.matp + (int64_t)a.emat_g[egrid] * LAMP;
+        if constexpr (kAdj) {  // K_e^0: the stiffness factor is applied to the line's forces
+          for (int c = j; c < LAMP; c += CTA_THREADS / 32) lsm[c * CTA_ELEMS + lane] = mp[c];
+        } else {
+          const float2 kp = bc2(a.ekeep_g[egrid]);
+          for (int c = j; c < LAMP; c += CTA_THREADS / 32) lsm[c * CTA_ELEMS + lane] = mul2(mp[c], kp);
+        }
+      }
       // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
       if (valid) {
         const float* urow = ub + slot(j) * 5 * W + 5 * q;
@@ -356,18 +369,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
           for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
         }
-        float2 L[LAMP];
-        {
-          const float2* mp = a.matp + (int64_t)a.emat_g[egrid] * LAMP;
-          if constexpr (kAdj) {  // K_e^0: the stiffness factor is applied to the line's forces
-#pragma unroll
-            for (int c = 0; c < LAMP; ++c) L[c] = mp[c];
-          } else {
-            const float2 kp = bc2(a.ekeep_g[egrid]);
-#pragma unroll
-            for (int c = 0; c < LAMP; ++c) L[c] = mul2(mp[c], kp);
-          }
-        }
+        const float2* L = lsm + lane;  // pair c at L[c * CTA_ELEMS]
         float2 Fe2[5][3];
 #pragma unroll
         for (int f = 0; f < 5; ++f)
@@ -386,26 +388,26 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           const float kx = gx[1], ky = gy[3], kxy = gy[1] + gx[3];
           const float gyz = v[3][k] + gy[4];
           const float gxz = v[1][k] + gx[4];
-          float2 NN = mul2(L[0], bc2(ex_));
-          NN = fma2(L[1], bc2(ey_), NN);
-          NN = fma2(L[2], bc2(gxy), NN);
-          NN = fma2(L[3], bc2(kx), NN);
-          NN = fma2(L[4], bc2(ky), NN);
-          NN = fma2(L[5], bc2(kxy), NN);          // (Nxx, Nyy)
-          float2 NM = mul2(L[6], bc2(ex_));
-          NM = fma2(L[7], bc2(ey_), NM);
-          NM = fma2(L[8], bc2(gxy), NM);
-          NM = fma2(L[9], bc2(kx), NM);
-          NM = fma2(L[10], bc2(ky), NM);
-          NM = fma2(L[11], bc2(kxy), NM);         // (Nxy, Mxx)
-          float2 MM = mul2(L[12], bc2(ex_));
-          MM = fma2(L[13], bc2(ey_), MM);
-          MM = fma2(L[14], bc2(gxy), MM);
-          MM = fma2(L[15], bc2(kx), MM);
-          MM = fma2(L[16], bc2(ky), MM);
-          MM = fma2(L[17], bc2(kxy), MM);         // (Myy, Mxy)
-          float2 QQ = mul2(L[18], bc2(gyz));
-          QQ = fma2(L[19], bc2(gxz), QQ);         // (Qy, Qx)
+          float2 NN = mul2(L[0 * CTA_ELEMS], bc2(ex_));
+          NN = fma2(L[1 * CTA_ELEMS], bc2(ey_), NN);
+          NN = fma2(L[2 * CTA_ELEMS], bc2(gxy), NN);
+          NN = fma2(L[3 * CTA_ELEMS], bc2(kx), NN);
+          NN = fma2(L[4 * CTA_ELEMS], bc2(ky), NN);
+          NN = fma2(L[5 * CTA_ELEMS], bc2(kxy), NN);          // (Nxx, Nyy)
+          float2 NM = mul2(L[6 * CTA_ELEMS], bc2(ex_));
+          NM = fma2(L[7 * CTA_ELEMS], bc2(ey_), NM);
+          NM = fma2(L[8 * CTA_ELEMS], bc2(gxy), NM);
+          NM = fma2(L[9 * CTA_ELEMS], bc2(kx), NM);
+          NM = fma2(L[10 * CTA_ELEMS], bc2(ky), NM);
+          NM = fma2(L[11 * CTA_ELEMS], bc2(kxy), NM);         // (Nxy, Mxx)
+          float2 MM = mul2(L[12 * CTA_ELEMS], bc2(ex_));
+          MM = fma2(L[13 * CTA_ELEMS], bc2(ey_), MM);
+          MM = fma2(L[14 * CTA_ELEMS], bc2(gxy), MM);
+          MM = fma2(L[15 * CTA_ELEMS], bc2(kx), MM);
+          MM = fma2(L[16 * CTA_ELEMS], bc2(ky), MM);
+          MM = fma2(L[17 * CTA_ELEMS], bc2(kxy), MM);         // (Myy, Mxy)
+          float2 QQ = mul2(L[18 * CTA_ELEMS], bc2(gyz));
+          QQ = fma2(L[19 * CTA_ELEMS], bc2(gxz), QQ);         // (Qy, Qx)
           const float Wn = c_w32[i] * c_w32[k] * t_area4;
           const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
           // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
