@@ -33,6 +33,10 @@ ALG_BYTES = {32: 16.0, 64: 32.0}   # algorithmic bytes per DOF-step (u_n, u_n-1,
 # capture in profiles/k_struct_step_f32_batch64_v4.md (292.9 + 83.5 MB for the
 # 64-plate batch of 30 001 270 DOF); traffic grows with the DOF count
 F32_TRAFFIC_PER_DOF = (292.914176e6 + 83.467264e6) / 30001270
+# floating-point operations per DOF-step of k_struct_step_f32, counted by ncu on the
+# same launch (sm__sass_thread_inst_executed_op_*: 706.5 M FFMA2 x 4, 170.4 M FMUL2 x 2,
+# 78.6 M FFMA x 2, 48.8 M FMUL, 82.9 M FADD) over 30 001 270 DOF
+F32_FLOP_PER_DOF = (706.536432e6 * 4 + 170.43642e6 * 2 + 78.595604e6 * 2 + 48.797086e6 + 82.893812e6) / 30001270
 METRIC = "DOF-steps/s (batched flat-shell SEM forward, 512 uneven plates)"
 
 
@@ -442,6 +446,9 @@ def main():
             "traffic": (F32_TRAFFIC_PER_DOF * ndof if args.precision == 32 and plan.info["path"] == 2 else None),
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 64-plate "
                               "batch, scaled by DOF (bytes per launch)",
+            "fp32_tflops": (F32_FLOP_PER_DOF * value / 1e12 if args.precision == 32 and plan.info["path"] == 2
+                            else None),
+            "flop_per_dof_step": F32_FLOP_PER_DOF if args.precision == 32 else None,
             "basis": f"{ALG_BYTES[args.precision]:.0f} B/DOF-step x {ndof} DOF per launch of "
                      f"k_struct_step, CUDA events over {args.steps} launches; peak {pk_kind}"}
     launches = args.steps * plan.info["launches_per_step"] + (args.steps // args.graph if args.graph else 1)
@@ -464,8 +471,11 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, used, tt = cpu_reference(scs, run, 10, budget_s=15.0)
+        v1, used1, tt1 = cpu_reference(scs[:2], run, 3, nthreads=1, budget_s=5.0)
         cpu = {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"first {used} plates x 10 time steps ({tt:.1f} s), FP64 oracle, all host threads"}
+               "sample": f"first {used} plates x 10 time steps ({tt:.1f} s), FP64 oracle, all host threads",
+               "single_core_value": v1,
+               "single_core_sample": f"first {used1} plates x 3 time steps ({tt1:.1f} s), one thread"}
     plan.close()
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
