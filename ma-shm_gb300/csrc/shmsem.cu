@@ -392,6 +392,7 @@ struct shm_plan {
   bool sp_generic = false;  // FP32 structured: use the generic template instead of the packed kernel
   // adjoint buffers (allocated by the first shm_forward_backward)
   void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr, *F2adj = nullptr;
+  void* gbox = nullptr;  // 3D solid plans of axis-aligned box elements: [4][fen_pad]
   cudaStream_t aux[2] = {nullptr, nullptr};  // adjoint: recompute and adjoint streams
   // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
@@ -2201,7 +2202,11 @@ static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.blowup = (T)p->blowup;
   a.flag = p->flag;
   a.d_base = p->d_base;
-  k_elem_solid<T><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
+  a.gbox = (const T*)p->gbox;
+  if (p->gbox)
+    k_elem_solid<T, true><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
+  else
+    k_elem_solid<T, false><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
   k_node_solid<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kstep);
   return cudaGetLastError();
 }
@@ -2209,7 +2214,8 @@ static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
 template <typename T>
 static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const std::vector<double>& geo,
                                const std::vector<int>& emat, const std::vector<double>& ekeep,
-                               const std::vector<double>& mat, const std::vector<double>& minv) {
+                               const std::vector<double>& mat, const std::vector<double>& minv,
+                               const std::vector<double>* gbox) {
   auto conv = [](const std::vector<double>& v) {
     std::vector<T> o(v.size());
     for (size_t i = 0; i < v.size(); ++i) o[i] = (T)v[i];
@@ -2219,7 +2225,13 @@ static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const 
   T *g = nullptr, *k = nullptr, *m = nullptr, *mi = nullptr, *ua = nullptr, *ub = nullptr, *f2 = nullptr,
     *fr = nullptr;
   if ((s = upload(p, &p->conn, conn)) != SHM_OK) return s;
-  if ((s = upload(p, &g, conv(geo))) != SHM_OK) return s;
+  if (gbox) {  // box elements: the per-node geometry is not needed on the device
+    T* gb = nullptr;
+    if ((s = upload(p, &gb, conv(*gbox))) != SHM_OK) return s;
+    p->gbox = gb;
+  } else if ((s = upload(p, &g, conv(geo))) != SHM_OK) {
+    return s;
+  }
   if ((s = upload(p, &p->emat, emat)) != SHM_OK) return s;
   if ((s = upload(p, &k, conv(ekeep))) != SHM_OK) return s;
   if ((s = upload(p, &m, conv(mat))) != SHM_OK) return s;
@@ -2311,6 +2323,13 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
     CKP(p, cudaMemcpyToSymbol(c_D32, D32, sizeof(float) * 36));
     CKP(p, cudaMemcpyToSymbol(c_D3_64, D3.data(), sizeof(double) * 9));
     CKP(p, cudaMemcpyToSymbol(c_D3_32, D332, sizeof(float) * 9));
+    float w32[NP], w332[S_NZ];
+    for (int i = 0; i < NP; ++i) w32[i] = (float)gw[i];
+    for (int i = 0; i < S_NZ; ++i) w332[i] = (float)gw3[i];
+    CKP(p, cudaMemcpyToSymbol(c_w64, gw.data(), sizeof(double) * NP));
+    CKP(p, cudaMemcpyToSymbol(c_w32, w32, sizeof(float) * NP));
+    CKP(p, cudaMemcpyToSymbol(c_w3_64, gw3.data(), sizeof(double) * S_NZ));
+    CKP(p, cudaMemcpyToSymbol(c_w3_32, w332, sizeof(float) * S_NZ));
   }
   const int64_t FP = p->fen_pad;
   std::vector<int> conn((size_t)S_NPE * FP, 0), emat(FP, 0);
@@ -2452,8 +2471,32 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
     minv[g] = mm > 0 ? 1.0 / mm : 0.0;
     for (int f = 0; f < 3; ++f) p->mass[3 * g + f] = mm;
   }
-  shm_status st = p->prec == 64 ? solid_device<double>(p, conn, geo, emat, ekeep, mat, minv)
-                                : solid_device<float>(p, conn, geo, emat, ekeep, mat, minv);
+  // axis-aligned boxes: diagonal constant inverse Jacobian and constant |det J|
+  // per element (4 numbers instead of 1 080 per-node values)
+  std::vector<double> gbox((size_t)4 * FP, 0.0);
+  bool box = true;
+  for (int64_t e = 0; e < p->fen && box; ++e) {
+    auto G = [&](int q, int c) { return geo[((int64_t)q * S_NPE + c) * FP + e]; };
+    const double s0 = G(0, 0), s1 = G(4, 0), s2 = G(8, 0);
+    const double v0 = G(9, 0) / (gw[0] * gw[0] * gw3[0]);
+    const double scale = std::fabs(s0) + std::fabs(s1) + std::fabs(s2);
+    for (int c = 0; c < S_NPE && box; ++c) {
+      const int cx = c % NP, cy = (c / NP) % NP, cz = c / 36;
+      for (int q = 0; q < 9; ++q)
+        if (q != 0 && q != 4 && q != 8 && std::fabs(G(q, c)) > 1e-12 * scale) box = false;
+      if (std::fabs(G(0, c) - s0) > 1e-10 * std::fabs(s0) || std::fabs(G(4, c) - s1) > 1e-10 * std::fabs(s1) ||
+          std::fabs(G(8, c) - s2) > 1e-10 * std::fabs(s2))
+        box = false;
+      const double v = G(9, c) / (gw[cx] * gw[cy] * gw3[cz]);
+      if (std::fabs(v - v0) > 1e-10 * std::fabs(v0)) box = false;
+    }
+    gbox[e] = s0;
+    gbox[FP + e] = s1;
+    gbox[2 * FP + e] = s2;
+    gbox[3 * FP + e] = v0;
+  }
+  shm_status st = p->prec == 64 ? solid_device<double>(p, conn, geo, emat, ekeep, mat, minv, box ? &gbox : nullptr)
+                                : solid_device<float>(p, conn, geo, emat, ekeep, mat, minv, box ? &gbox : nullptr);
   if (st != SHM_OK) return st;
   if ((st = upload(p, &p->row_ptr, row_ptr)) != SHM_OK) return st;
   if ((st = upload(p, &p->slots, slots)) != SHM_OK) return st;

@@ -25,6 +25,11 @@ constexpr int S_MAT_DEV = 16;
 
 static __constant__ double c_D3_64[S_NZ * S_NZ];
 static __constant__ float c_D3_32[S_NZ * S_NZ];
+static __constant__ double c_w3_64[S_NZ];
+static __constant__ float c_w3_32[S_NZ];
+template <typename T> __device__ __forceinline__ T W3m(int r);
+template <> __device__ __forceinline__ double W3m<double>(int r) { return c_w3_64[r]; }
+template <> __device__ __forceinline__ float W3m<float>(int r) { return c_w3_32[r]; }
 template <typename T> __device__ __forceinline__ T D3m(int r, int c);
 template <> __device__ __forceinline__ double D3m<double>(int r, int c) { return c_D3_64[r * S_NZ + c]; }
 template <> __device__ __forceinline__ float D3m<float>(int r, int c) { return c_D3_32[r * S_NZ + c]; }
@@ -37,6 +42,7 @@ template <typename T> struct SolidArgs {
   T* F2;                           // [3][plane], element slots c*fen_pad + e, then force slots
   const int* __restrict__ conn;    // [108][fen_pad]
   const T* __restrict__ geo;       // [10][108][fen_pad]: invJ_ab (a = xi,eta,zeta; b = x,y,z) row-major, W
+  const T* __restrict__ gbox;      // box elements: [4][fen_pad] dxi/dx, deta/dy, dzeta/dz, |det J|
   const int* __restrict__ emat;
   const T* __restrict__ ekeep;
   const T* __restrict__ mat;       // [nmat][16]
@@ -60,7 +66,11 @@ template <typename T> struct SolidArgs {
   const int* d_base;
 };
 
-template <typename T>
+// kBox: every element is an axis-aligned box, so the inverse Jacobian is the
+// constant diagonal (sx, sy, sz) and w_i w_j w_k |det J| the weights times a
+// constant volume factor: four numbers per element replace the 1 080 per-node
+// geometry values.
+template <typename T, bool kBox>
 __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int kstep) {
   __shared__ T su[S_EPB][3][S_NPE];
   __shared__ T sg[S_EPB][9][S_NPE];   // flux of field f along direction d at [f*3+d]
@@ -102,15 +112,26 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
     d[f][2] = sz;
   }
   T iJ[3][3];
+  T W;
+  if constexpr (kBox) {
 #pragma unroll
-  for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * S_NPE + c) * a.fen_pad + e];
-  const T W = a.geo[((int64_t)9 * S_NPE + c) * a.fen_pad + e];
+    for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = T(0);
+    iJ[0][0] = a.gbox[e];
+    iJ[1][1] = a.gbox[a.fen_pad + e];
+    iJ[2][2] = a.gbox[2 * a.fen_pad + e];
+    W = Wg<T>(cx) * Wg<T>(cy) * W3m<T>(cz) * a.gbox[3 * a.fen_pad + e];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * S_NPE + c) * a.fen_pad + e];
+    W = a.geo[((int64_t)9 * S_NPE + c) * a.fen_pad + e];
+  }
   // physical gradient g[f][b] = sum_a d[f][a] * invJ_ab  (strains_spec_p.m)
   T g[3][3];
 #pragma unroll
   for (int f = 0; f < 3; ++f)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) g[f][b] = d[f][0] * iJ[0][b] + d[f][1] * iJ[1][b] + d[f][2] * iJ[2][b];
+    for (int b = 0; b < 3; ++b)
+      g[f][b] = kBox ? d[f][b] * iJ[b][b] : d[f][0] * iJ[0][b] + d[f][1] * iJ[1][b] + d[f][2] * iJ[2][b];
   const T Exx = g[0][0], Eyy = g[1][1], Ezz = g[2][2];
   const T Exy = g[0][1] + g[1][0];
   const T Eyz = g[1][2] + g[2][1];
@@ -133,7 +154,8 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
   for (int f = 0; f < 3; ++f)
 #pragma unroll
     for (int aa = 0; aa < 3; ++aa)
-      sg[le][f * 3 + aa][c] = W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
+      sg[le][f * 3 + aa][c] = kBox ? W * (S[f][aa] * iJ[aa][aa])
+                                   : W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
   __syncthreads();
   // transposed operators: Npx' (xi), Npy' (eta), Npz' (zeta)
 #pragma unroll
