@@ -1,7 +1,8 @@
 """Oracle driver: builds ``sem_oracle.c`` and runs the FP64 reference restatement.
 
 TEST INFRASTRUCTURE ONLY (tests/, __graft_entry__.smoke(), bench.py's CPU
-baseline / reference arm).  All set-up quantities are recomputed here from
+baseline / reference arm).  Parity unpinned for the time loop (no reference
+golden outputs exist); set-up constants are pinned in tests/golden/.  All set-up quantities are recomputed here from
 the restated reference functions in ``ref_setup.py``; nothing is taken from
 the product except the raw inputs (mesh arrays, material table, signal).
 """

@@ -3,7 +3,8 @@
  * explicit central-difference loop.
  *
  * TEST INFRASTRUCTURE ONLY.  The product never links, loads or calls this
- * file.  tests/ use it as the checker, bench.py's --impl reference arm and
+ * file.  Parity unpinned: the reference has no golden outputs for this loop
+ * (only its set-up constants are pinned, see tests/golden/).  tests/ use it as the checker, bench.py's --impl reference arm and
  * cpu_baseline leg time it as the reference's CPU path (the MATLAB original
  * cannot run without MATLAB).
  *
