@@ -39,6 +39,8 @@ template <typename T> struct GenArgs {
   T* UA;
   T* UB;
   T* outp;                        // u_{n+1} destination; null = over u_{n-1} (ping-pong)
+  const T* __restrict__ grect;    // [3][fen_pad] 2/ax, 2/ay, ax*ay/4 when every element is an
+                                  // axis-aligned rectangle (else null: per-node geometry)
   T* F2;
   // mesh
   const int* __restrict__ conn;   // [36][fen_pad], 0-based global nodes
@@ -95,7 +97,7 @@ __device__ __forceinline__ void block0_duties(const GenArgs<T>& a, const T* cur,
     a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
 }
 
-template <typename T, bool kSensor>
+template <typename T, bool kSensor, bool kRect = false>
 __global__ void __launch_bounds__(CTA_THREADS) k_elem_general(GenArgs<T> a, int kstep) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
@@ -131,9 +133,15 @@ __global__ void __launch_bounds__(CTA_THREADS) k_elem_general(GenArgs<T> a, int 
 #pragma unroll
       for (int k = 0; k < NP; ++k) v[f][k] = xs[f * NPE + i * NP + k];
     const Lam<T> L = load_lam(a.mat + (int64_t)a.emat[e] * MAT_STRIDE_DEV, a.ekeep[e]);
-    GeoGeneral<T> geo{a.geo, a.fen_pad, e};
     T Fe[5][NP];
-    const T vp = shell_column<T, GeoGeneral<T>, kSensor>(v, ys, xs, i, L, geo, Fe, a.sc);
+    T vp;
+    if constexpr (kRect) {  // three numbers per element instead of 180 per-node values
+      const GeoRect<T> geo{a.grect[e], a.grect[a.fen_pad + e], a.grect[2 * a.fen_pad + e]};
+      vp = shell_column<T, GeoRect<T>, kSensor>(v, ys, xs, i, L, geo, Fe, a.sc);
+    } else {
+      const GeoGeneral<T> geo{a.geo, a.fen_pad, e};
+      vp = shell_column<T, GeoGeneral<T>, kSensor>(v, ys, xs, i, L, geo, Fe, a.sc);
+    }
 #pragma unroll
     for (int f = 0; f < 5; ++f)
 #pragma unroll
@@ -393,6 +401,7 @@ struct shm_plan {
   // adjoint buffers (allocated by the first shm_forward_backward)
   void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr, *F2adj = nullptr;
   void* gbox = nullptr;  // 3D solid plans of axis-aligned box elements: [4][fen_pad]
+  void* grect = nullptr; // flat-shell plans of axis-aligned rectangles: [3][fen_pad]
   cudaStream_t aux[2] = {nullptr, nullptr};  // adjoint: recompute and adjoint streams
   // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
@@ -615,6 +624,7 @@ template <typename T> static GenArgs<T> make_args(shm_plan* p) {
   a.UA = (T*)(p->ov_UA ? p->ov_UA : p->UA);
   a.UB = (T*)(p->ov_UB ? p->ov_UB : p->UB);
   a.outp = (T*)p->ov_out;
+  a.grect = (const T*)p->grect;
   a.F2 = (T*)p->F2;
   a.conn = p->conn;
   a.geo = (const T*)p->geo;
@@ -666,10 +676,16 @@ static cudaError_t launch_general_step(shm_plan* p, int kstep, cudaStream_t s) {
   GenArgs<T> a = make_args<T>(p);
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   const size_t sm = elem_smem_bytes(sizeof(T) == 8 ? 64 : 32);
-  if (p->nslot > 0)
+  if (p->grect) {
+    if (p->nslot > 0)
+      k_elem_general<T, true, true><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
+    else
+      k_elem_general<T, false, true><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
+  } else if (p->nslot > 0) {
     k_elem_general<T, true><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
-  else
+  } else {
     k_elem_general<T, false><<<nblk, CTA_THREADS, sm, s>>>(a, kstep);
+  }
   k_node_general<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kstep);
   return cudaGetLastError();
 }
@@ -693,6 +709,10 @@ static shm_status set_func_attrs(shm_plan* p) {
   CKP(p, cudaFuncSetAttribute(k_elem_general<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
   CKP(p, cudaFuncSetAttribute(k_elem_general<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
   CKP(p, cudaFuncSetAttribute(k_elem_general<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+  CKP(p, cudaFuncSetAttribute(k_elem_general<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
   CKP(p, cudaFuncSetAttribute(k_elem_adjoint<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)adj_smem_bytes(64)));
   CKP(p, cudaFuncSetAttribute(k_elem_adjoint<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1398,6 +1418,24 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
   for (int64_t g = 0; g < p->nnode; ++g)
     if (fillc[g] != node_cnt[g]) return bad(p, "mesh: basket maps do not cover every element node");
 
+  // axis-aligned rectangles: invJ = diag(2/ax, 2/ay) and det J = ax ay / 4 on
+  // every node of every element (then the element kernel reads 3 numbers)
+  std::vector<double> grect((size_t)3 * FP, 0.0);
+  bool rect = p->fen > 0;
+  for (int64_t e = 0; e < p->fen && rect; ++e) {
+    auto G = [&](int q, int c) { return geo[(int64_t)q * NPE * FP + (int64_t)c * FP + e]; };
+    const double sx = G(0, 0), sy = G(3, 0), a4 = G(4, 0) / (gw[0] * gw[0]);
+    for (int c = 0; c < NPE && rect; ++c) {
+      if (std::fabs(G(1, c)) > 1e-12 * std::fabs(sx) || std::fabs(G(2, c)) > 1e-12 * std::fabs(sy) ||
+          std::fabs(G(0, c) - sx) > 1e-10 * std::fabs(sx) || std::fabs(G(3, c) - sy) > 1e-10 * std::fabs(sy) ||
+          std::fabs(G(4, c) / (gw[c % NP] * gw[c / NP]) - a4) > 1e-10 * std::fabs(a4))
+        rect = false;
+    }
+    grect[e] = sx;
+    grect[FP + e] = sy;
+    grect[2 * FP + e] = a4;
+  }
+
   // diagonal mass (main_flat_shell.m:493-501), summed in basket order
   std::vector<double> minv((size_t)2 * p->nnode_pad, 0.0), area((size_t)p->nnode_pad, 0.0);
   p->mass.assign((size_t)5 * p->nnode, 0.0);
@@ -1468,6 +1506,18 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
   if ((st = upload(p, &p->out_node, out_node)) != SHM_OK) return st;
   if ((st = upload(p, &p->out_field, out_field)) != SHM_OK) return st;
   if ((st = upload(p, &p->esens, esens)) != SHM_OK) return st;
+  if (rect) {
+    if (p->prec == 64) {
+      double* gr = nullptr;
+      if ((st = upload(p, &gr, grect)) != SHM_OK) return st;
+      p->grect = gr;
+    } else {
+      std::vector<float> g32(grect.begin(), grect.end());
+      float* gr = nullptr;
+      if ((st = upload(p, &gr, g32)) != SHM_OK) return st;
+      p->grect = gr;
+    }
+  }
   if ((st = upload(p, &p->sptr, sptr)) != SHM_OK) return st;
   if ((st = dalloc(p, &p->st, (size_t)nscen * p->nft)) != SHM_OK) return st;
   if ((st = dalloc(p, &p->displ, (size_t)std::max(p->nout, 1) * p->nft)) != SHM_OK) return st;
