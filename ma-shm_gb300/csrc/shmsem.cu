@@ -1908,6 +1908,27 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
 // discrete adjoint: misfit gradient with respect to per-element damage
 // ---------------------------------------------------------------------------
 
+// Scope guards: device buffers and events released on every return path.
+struct DevFree {
+  void* p = nullptr;
+  ~DevFree() {
+    if (p) cudaFree(p);
+  }
+};
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  cudaEvent_t add(unsigned flags = cudaEventDefault) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, flags);
+    ev.push_back(e);
+    return e;
+  }
+  ~EventSet() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
 template <typename T>
 static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target, double* misfit, double* grad,
                             int k, cudaStream_t s) {
@@ -1944,14 +1965,16 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   T* ck = (T*)p->ck;
   T* seg = (T*)p->seg;
   const size_t SB = S * sizeof(T);
+  EventSet evs;
   cudaEvent_t ev[4];
-  for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
+  for (int i = 0; i < 4; ++i) ev[i] = evs.add();
   float t_rec = 0.f, t_adj = 0.f;
   // the last `nstore` segments keep every state of the forward pass in spare
   // device memory (8 GiB left free), so the backward pass recomputes only the
   // others
   int nstore = 0;
   T* store = nullptr;
+  DevFree store_guard;
   {
     size_t fr = 0, tot = 0;
     const size_t per = (size_t)k * SB;
@@ -1963,8 +1986,10 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     }
     while (nstore > 0 && cudaMalloc(&store, (size_t)nstore * k * SB) != cudaSuccess) {
       cudaGetLastError();
+      store = nullptr;
       nstore /= 2;
     }
+    store_guard.p = store;
   }
   const int jstore = nck - nstore;  // first stored segment
   p->last_nstore = nstore;
@@ -2001,7 +2026,6 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
       cudaError_t e = launch_step(p, i, s);
       p->ov_UA = p->ov_UB = p->ov_out = nullptr;
       if (e != cudaSuccess) {
-        if (store) cudaFree(store);
         p->err = std::string("forward: ") + cudaGetErrorString(e);
         return SHM_ERR_CUDA;
       }
@@ -2048,14 +2072,12 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   CKP(p, cudaMemsetAsync(p->F2adj, 0, sizeof(T) * 5 * p->plane, s));
   CKP(p, cudaMemsetAsync(p->grad, 0, sizeof(double) * p->fen_pad, s));
   CKP(p, cudaMemcpyAsync(p->d_base_adj, &n0, 4, cudaMemcpyHostToDevice, s));
-  cudaEvent_t ev_s, ev_end_r, ev_end_a;
+  const cudaEvent_t ev_s = evs.add(cudaEventDisableTiming);
+  const cudaEvent_t ev_end_r = evs.add(), ev_end_a = evs.add();
   std::vector<cudaEvent_t> evR(nck), evA(nck);
-  cudaEventCreateWithFlags(&ev_s, cudaEventDisableTiming);
-  cudaEventCreate(&ev_end_r);
-  cudaEventCreate(&ev_end_a);
   for (int j = 0; j < nck; ++j) {
-    cudaEventCreateWithFlags(&evR[j], cudaEventDisableTiming);
-    cudaEventCreateWithFlags(&evA[j], cudaEventDisableTiming);
+    evR[j] = evs.add(cudaEventDisableTiming);
+    evA[j] = evs.add(cudaEventDisableTiming);
   }
   CKP(p, cudaEventRecord(ev_s, s));
   CKP(p, cudaStreamWaitEvent(sr, ev_s, 0));
@@ -2157,15 +2179,6 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
   CKP(p, cudaStreamSynchronize(s));
   cudaEventElapsedTime(&t_rec, ev[2], ev_end_r);
   cudaEventElapsedTime(&t_adj, ev[3], ev_end_a);
-  if (store) cudaFree(store);
-  cudaEventDestroy(ev_s);
-  cudaEventDestroy(ev_end_r);
-  cudaEventDestroy(ev_end_a);
-  for (int j = 0; j < nck; ++j) {
-    cudaEventDestroy(evR[j]);
-    cudaEventDestroy(evA[j]);
-  }
-  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   p->fb_ms[0] = t_fwd;
   p->fb_ms[1] = t_rec;
   p->fb_ms[2] = t_adj;
