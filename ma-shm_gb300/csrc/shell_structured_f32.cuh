@@ -295,12 +295,14 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
     int rb6 = 0;  // r mod 6
     for (int r = 0; r < maxrows; ++r) {
-      // next element row's five new node rows (ring slots free since row r-1):
-      // node rows 5r+6 .. 5r+10 go to slots (rb + 6) mod 11 onwards
+      // this row's node rows have landed (the only copy group in flight); the
+      // barrier also ends the previous row's update for every warp, so the
+      // ring slots of the previous row's first five node rows are free: the
+      // next element row's five new node rows (5r+6 .. 5r+10) go there
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncthreads();
       if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
       cp_async_commit();
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-      __syncthreads();
 
       const bool rowact = r < t_nrows;
       const bool valid = rowact && colok;
@@ -607,8 +609,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             }
           }
         }
-      // ring slots read above are refilled by the next row's prefetch
-      __syncthreads();
+      // (the next row's first barrier separates this update from the ring
+      // refill and the next band accumulation)
       rb += 5;
       if (rb >= UR) rb -= UR;
       if (++rb6 == 6) rb6 = 0;
