@@ -542,7 +542,15 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             for (int f = 0; f < 5; ++f) dst[f * W + 5] = out[f][5];
           }
         }
-        __syncthreads();
+        // band row j is now complete and written by this warp alone (row 0
+        // adds the previous element row's line 5, stored before this row's
+        // first barrier), and warp j updates exactly band row j: a warp
+        // barrier suffices.  The adjoint's gradient partials (vred) are
+        // reduced across warps below and need the CTA barrier.
+        if constexpr (kAdj)
+          __syncthreads();
+        else
+          __syncwarp();
       }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
       if (kAdj && j == 0 && valid && owned_row && q > 0) {
