@@ -404,7 +404,7 @@ def main():
             cpu_reference(scs[:1], run, 3)
         v, used, tt = cpu_reference(scs, run, steps, budget_s=20.0)
         out = {"metric": METRIC, "value": v, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "warmup": args.warmup, "ms_per_step": 1e3 * ndof / v, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
                "cpu_baseline": {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"first {used} plates x {steps} time steps, FP64 oracle restating "
