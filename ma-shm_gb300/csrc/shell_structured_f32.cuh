@@ -247,6 +247,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   // owned columns c = lane + 32*s
   float uo_r[G][NCOL][5];
   float mt_r[G][NCOL], mr_r[G][NCOL];
+  bool gpend = false;      // adjoint: an element's gradient partials await reduction
+  long long gpend_e = 0;   // (its grid-order index)
 
   __shared__ GroupTask gt[G];  // task facts of the lane groups (shared, not in registers)
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
@@ -301,6 +303,13 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       // next element row's five new node rows (5r+6 .. 5r+10) go there
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       __syncthreads();
+      if (kAdj && gpend) {  // previous element row's gradient partials are complete
+        double sum = 0.0;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
+        a.grad[a.e_of_g[gpend_e]] -= sum;
+        gpend = false;
+      }
       if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
       cp_async_commit();
 
@@ -545,19 +554,14 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         // band row j is now complete and written by this warp alone (row 0
         // adds the previous element row's line 5, stored before this row's
         // first barrier), and warp j updates exactly band row j: a warp
-        // barrier suffices.  The adjoint's gradient partials (vred) are
-        // reduced across warps below and need the CTA barrier.
-        if constexpr (kAdj)
-          __syncthreads();
-        else
-          __syncwarp();
+        // barrier suffices.  (The adjoint's gradient partials are reduced
+        // after the next CTA barrier.)
+        __syncwarp();
       }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
-      if (kAdj && j == 0 && valid && owned_row && q > 0) {
-        double sum = 0.0;
-#pragma unroll
-        for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
-        a.grad[a.e_of_g[egrid]] -= sum;
+      if (kAdj && j == 0) {  // reduced after the next CTA barrier
+        gpend = valid && owned_row && q > 0;
+        gpend_e = egrid;
       }
       if (kSensor && j == 0 && valid && owned_row && q > 0) {
         const int sl = a.esens_g[egrid];
@@ -625,6 +629,13 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     }
     cp_async_wait_all();
     __syncthreads();
+    if (kAdj && gpend) {  // the task's last element row
+      double sum = 0.0;
+#pragma unroll
+      for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
+      a.grad[a.e_of_g[gpend_e]] -= sum;
+      gpend = false;
+    }
   }
   if (bad) atomicOr(a.flag, 1);
 }
