@@ -363,3 +363,22 @@ def test_unstructured_quad_mesh_matches_oracle(pkg, precision):
     _, ref = oracle_run(sc, run)
     assert np.abs(ref["displ"]).max() > 0
     assert rel(got["displ"], ref["displ"]) <= (FP64_TOL if precision == 64 else FP32_TOL)
+
+
+@pytest.mark.parametrize("precision,path", [(64, 2), (32, 2), (64, 1)])
+def test_all_frame_fields_match_oracle(pkg, precision, path):
+    """Frames of displacement, velocity and acceleration of all five DOF
+    components (field_variable 'all') from every kind of step kernel."""
+    scs, run = small_case(pkg, nex=6, ney=5)
+    run.frm_int, run.frame_dof, run.frame_kind = 37, 0, 3
+    plan = pkg.Plan(scs, run, precision=precision, path=path)
+    assert plan.info["path"] == path and plan.info["nfields"] == 15
+    got = plan.forward(want_frames=True)[0]["frames"]
+    plan.close()
+    _, ref = oracle_run(scs[0], run)
+    assert got.shape == ref["frames"].shape
+    tols = (FP64_TOL,) * 3 if precision == 64 else (FP32_TOL, FP32_TOL, 1e-2)
+    for kind in range(3):
+        sl = slice(5 * kind, 5 * kind + 5)
+        assert np.abs(ref["frames"][:, sl]).max() > 0
+        assert rel(got[:, sl], ref["frames"][:, sl]) <= tols[kind], kind
