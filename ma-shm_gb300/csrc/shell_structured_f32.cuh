@@ -11,7 +11,10 @@
 //  * the force band is a 6-row ring (the shared node row is carried by
 //    re-labelling, not copied);
 //  * the update's loads of u_{n-1} and 1/M are issued before phase C so that
-//    their latency overlaps the transposed operator.
+//    their latency overlaps the transposed operator;
+//  * the laminate pairs are copied with cp.async one row ahead
+//    (double-buffered); the material index is read two rows ahead and the
+//    stiffness factor one row ahead into registers.
 // Results equal the generic kernel's up to FP32 rounding order.
 #pragma once
 #include <cuda_fp16.h>
@@ -59,7 +62,7 @@ template <int EW>
 constexpr size_t struct_f32_smem_bytes() {
   using GM = F32Geom<EW>;
   return sizeof(float) * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS + GM::G * (GM::UGS + GM::FGS)) +
-         sizeof(float2) * LAMP * CTA_ELEMS;
+         sizeof(float2) * 2 * LAMP * CTA_ELEMS;
 }
 
 struct F32Args {
@@ -222,7 +225,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
   float* ring = vred + NP * CTA_ELEMS;
   float* band = ring + G * GM::UGS;
-  // laminate pairs of the row's elements, [LAMP][lane] (staged by all warps in phase A)
+  // laminate pairs of a row's elements, two buffers [2][LAMP][lane] (row r in
+  // buffer r & 1, copied at the top of row r - 1)
   float2* lsm = reinterpret_cast<float2*>(band + G * GM::FGS);
 
   const int nn = *a.d_base + kstep;
@@ -249,6 +253,16 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float mt_r[G][NCOL], mr_r[G][NCOL];
   bool gpend = false;      // adjoint: an element's gradient partials await reduction
   long long gpend_e = 0;   // (its grid-order index)
+
+  // copy the lane's element's laminate pairs (warp j: pairs j, j+6, ...)
+  auto lam_load = [&](int buf, int mat) {
+    const float2* mp = a.matp + (int64_t)mat * LAMP;
+    float2* d = lsm + buf * LAMP * CTA_ELEMS + lane;
+    for (int c = j; c < LAMP; c += CTA_THREADS / 32) {
+      const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(d + c * CTA_ELEMS));
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(mp + c) : "memory");
+    }
+  };
 
   __shared__ GroupTask gt[G];  // task facts of the lane groups (shared, not in registers)
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
@@ -292,6 +306,15 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
     const unsigned colmask = ring_colmask<EW>(gt);
     ring_load<EW, 6>(ring, cur, a.nnode_pad, gt, 0, 0, colmask);
+    // row 0's laminate pairs; the material index two rows ahead and the
+    // stiffness factor one row ahead are read into registers
+    int mnext = 0;
+    float keep = 1.f, knext = 1.f;
+    if (t_nrows > 0 && colok) {
+      lam_load(0, a.emat_g[eg0]);
+      keep = a.ekeep_g[eg0];
+    }
+    if (t_nrows > 1 && colok) mnext = a.emat_g[eg0 + t_nex];
     cp_async_commit();
 
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
@@ -310,24 +333,20 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         a.grad[a.e_of_g[gpend_e]] -= sum;
         gpend = false;
       }
-      if (r + 1 < maxrows) ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
-      cp_async_commit();
-
       const bool rowact = r < t_nrows;
       const bool valid = rowact && colok;
       const long long egrid = eg0 + (long long)r * t_nex;
+      // the next row's laminate pairs go to the other buffer (last read in the
+      // previous row's phase B)
+      if (r + 1 < maxrows) {
+        ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
+        if (r + 1 < t_nrows && colok) lam_load((r + 1) & 1, mnext);
+      }
+      cp_async_commit();
+      if (r + 1 < t_nrows && colok) knext = a.ekeep_g[egrid + t_nex];
+      if (r + 2 < t_nrows && colok) mnext = a.emat_g[egrid + 2 * t_nex];
       auto slot = [rb](int k) { const int s = rb + k; return s >= UR ? s - UR : s; };
 
-      // stage the element's laminate pairs: warp j loads pairs j, j+6, ...
-      if (valid) {
-        const float2* mp = a.matp + (int64_t)a.emat_g[egrid] * LAMP;
-        if constexpr (kAdj) {  // K_e^0: the stiffness factor is applied to the line's forces
-          for (int c = j; c < LAMP; c += CTA_THREADS / 32) lsm[c * CTA_ELEMS + lane] = mp[c];
-        } else {
-          const float2 kp = bc2(a.ekeep_g[egrid]);
-          for (int c = j; c < LAMP; c += CTA_THREADS / 32) lsm[c * CTA_ELEMS + lane] = mul2(mp[c], kp);
-        }
-      }
       // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
       if (valid) {
         const float* urow = ub + slot(j) * 5 * W + 5 * q;
@@ -380,7 +399,9 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
           for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
         }
-        const float2* L = lsm + lane;  // pair c at L[c * CTA_ELEMS]
+        const float2* L = lsm + (r & 1) * LAMP * CTA_ELEMS + lane;  // pair c at L[c * CTA_ELEMS]
+        // the stiffness factor scales the element's fluxes (K_e^0 for the adjoint)
+        const float akeep = kAdj ? t_area4 : t_area4 * keep;
         float2 Fe2[5][3];
 #pragma unroll
         for (int f = 0; f < 5; ++f)
@@ -419,7 +440,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           MM = fma2(L[17 * CTA_ELEMS], bc2(kxy), MM);         // (Myy, Mxy)
           float2 QQ = mul2(L[18 * CTA_ELEMS], bc2(gyz));
           QQ = fma2(L[19 * CTA_ELEMS], bc2(gxz), QQ);         // (Qy, Qx)
-          const float Wn = c_w32[i] * c_w32[k] * t_area4;
+          const float Wn = c_w32[i] * c_w32[k] * akeep;
           const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
           // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
           const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
@@ -500,7 +521,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         if constexpr (kAdj) {
           // line j's share of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
           const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
-          const float keep = a.ekeep_g[egrid];
           float dl = 0.f;
 #pragma unroll
           for (int f = 0; f < 5; ++f)
@@ -623,6 +643,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         }
       // (the next row's first barrier separates this update from the ring
       // refill and the next band accumulation)
+      keep = knext;
       rb += 5;
       if (rb >= UR) rb -= UR;
       if (++rb6 == 6) rb6 = 0;
