@@ -39,6 +39,10 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 // (Myy,Mxy): (b12,b16) (b22,b26) (b26,b66) (d12,d16) (d22,d26) (d26,d66)
 // (Qy,Qx):   (a44,a45) (a45,a55)
 constexpr int LAMP = 20;
+#ifndef SHM_F32_KB
+#define SHM_F32_KB 3
+#endif
+constexpr int KB = SHM_F32_KB;  // column nodes per laminate read in phase B (divides 6)
 
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -408,63 +412,76 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
           for (int p = 0; p < 3; ++p) Fe2[f][p] = make_float2(0.f, 0.f);
         float vp = 0.f;
+        // nodes k of the column in blocks of KB: each laminate pair is read
+        // from shared memory once per block (the products keep their order)
 #pragma unroll
-        for (int k = 0; k < NP; ++k) {
-          float gx[5], gy[5];
+        for (int k0 = 0; k0 < NP; k0 += KB) {
+          // strains: ex, ey, gxy, kx, ky, kxy, gyz, gxz
+          float sn[KB][8];
 #pragma unroll
-          for (int f = 0; f < 5; ++f) {
-            gx[f] = ys[f * NPE + i * NP + k];
-            gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
+          for (int kk = 0; kk < KB; ++kk) {
+            const int k = k0 + kk;
+            float gx[5], gy[5];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+              gx[f] = ys[f * NPE + i * NP + k];
+              gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
+            }
+            sn[kk][0] = gx[0];
+            sn[kk][1] = gy[2];
+            sn[kk][2] = gy[0] + gx[2];
+            sn[kk][3] = gx[1];
+            sn[kk][4] = gy[3];
+            sn[kk][5] = gy[1] + gx[3];
+            sn[kk][6] = v[3][k] + gy[4];
+            sn[kk][7] = v[1][k] + gx[4];
+            if (kSensor) {
+              vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
+            }
           }
-          const float ex_ = gx[0], ey_ = gy[2], gxy = gy[0] + gx[2];
-          const float kx = gx[1], ky = gy[3], kxy = gy[1] + gx[3];
-          const float gyz = v[3][k] + gy[4];
-          const float gxz = v[1][k] + gx[4];
-          float2 NN = mul2(L[0 * CTA_ELEMS], bc2(ex_));
-          NN = fma2(L[1 * CTA_ELEMS], bc2(ey_), NN);
-          NN = fma2(L[2 * CTA_ELEMS], bc2(gxy), NN);
-          NN = fma2(L[3 * CTA_ELEMS], bc2(kx), NN);
-          NN = fma2(L[4 * CTA_ELEMS], bc2(ky), NN);
-          NN = fma2(L[5 * CTA_ELEMS], bc2(kxy), NN);          // (Nxx, Nyy)
-          float2 NM = mul2(L[6 * CTA_ELEMS], bc2(ex_));
-          NM = fma2(L[7 * CTA_ELEMS], bc2(ey_), NM);
-          NM = fma2(L[8 * CTA_ELEMS], bc2(gxy), NM);
-          NM = fma2(L[9 * CTA_ELEMS], bc2(kx), NM);
-          NM = fma2(L[10 * CTA_ELEMS], bc2(ky), NM);
-          NM = fma2(L[11 * CTA_ELEMS], bc2(kxy), NM);         // (Nxy, Mxx)
-          float2 MM = mul2(L[12 * CTA_ELEMS], bc2(ex_));
-          MM = fma2(L[13 * CTA_ELEMS], bc2(ey_), MM);
-          MM = fma2(L[14 * CTA_ELEMS], bc2(gxy), MM);
-          MM = fma2(L[15 * CTA_ELEMS], bc2(kx), MM);
-          MM = fma2(L[16 * CTA_ELEMS], bc2(ky), MM);
-          MM = fma2(L[17 * CTA_ELEMS], bc2(kxy), MM);         // (Myy, Mxy)
-          float2 QQ = mul2(L[18 * CTA_ELEMS], bc2(gyz));
-          QQ = fma2(L[19 * CTA_ELEMS], bc2(gxz), QQ);         // (Qy, Qx)
-          const float Wn = c_w32[i] * c_w32[k] * akeep;
-          const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
-          // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
-          const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
-          const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
-          const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
-          const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
-          const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
-          const float2 Gs[5] = {G0, G1, G2, G3, G4};
+          // R[0] = (Nxx, Nyy), R[1] = (Nxy, Mxx), R[2] = (Myy, Mxy), R[3] = (Qy, Qx)
+          float2 R[4][KB];
 #pragma unroll
-          for (int f = 0; f < 5; ++f) {
-            ys[f * NPE + i * NP + k] = Gs[f].x;
-            const float2 ge = bc2(Gs[f].y);
+          for (int b = 0; b < 3; ++b)
 #pragma unroll
-            for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
+            for (int c = 0; c < 6; ++c) {
+              const float2 l = L[(6 * b + c) * CTA_ELEMS];
+#pragma unroll
+              for (int kk = 0; kk < KB; ++kk)
+                R[b][kk] = c == 0 ? mul2(l, bc2(sn[kk][c])) : fma2(l, bc2(sn[kk][c]), R[b][kk]);
+            }
+          {
+            const float2 l18 = L[18 * CTA_ELEMS], l19 = L[19 * CTA_ELEMS];
+#pragma unroll
+            for (int kk = 0; kk < KB; ++kk) R[3][kk] = fma2(l19, bc2(sn[kk][7]), mul2(l18, bc2(sn[kk][6])));
           }
-          if (k & 1) {
-            Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
-            Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
-          } else {
-            Fe2[1][k >> 1].x += Wn * QQ.y;
-            Fe2[3][k >> 1].x += Wn * QQ.x;
-          }
-          if (kSensor) {
-            vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
+#pragma unroll
+          for (int kk = 0; kk < KB; ++kk) {
+            const int k = k0 + kk;
+            const float2 NN = R[0][kk], NM = R[1][kk], MM = R[2][kk], QQ = R[3][kk];
+            const float Wn = c_w32[i] * c_w32[k] * akeep;
+            const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
+            // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
+            const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
+            const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
+            const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
+            const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
+            const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
+            const float2 Gs[5] = {G0, G1, G2, G3, G4};
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+              ys[f * NPE + i * NP + k] = Gs[f].x;
+              const float2 ge = bc2(Gs[f].y);
+#pragma unroll
+              for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
+            }
+            if (k & 1) {
+              Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
+              Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
+            } else {
+              Fe2[1][k >> 1].x += Wn * QQ.y;
+              Fe2[3][k >> 1].x += Wn * QQ.x;
+            }
           }
         }
 #pragma unroll
