@@ -281,10 +281,15 @@ def single_plate_bench(pkg, args):
     else:
         scs, run = W.plate_force() if args.workload == "force" else W.plate_pzt()
         ndof = W.dof_count(scs)
+    if args.nft > 0:  # a shorter run of the same plate (profiling)
+        run.nft = min(run.nft, args.nft)
+        for sc in scs:
+            sc.signal = np.asarray(sc.signal)[:run.nft]
     nsteps = run.nft - run.nn_first + 1
     res, out = {}, {"workload": args.workload, "dof": ndof, "nft": run.nft, "dt_s": run.dt,
                     "frames": run.frm_int > 0}
-    for prec in (64, 32):
+    precs = (64, 32) if args.prec == 0 else (args.prec,)
+    for prec in precs:
         if args.workload == "solid":
             p = pkg.SolidPlan(scs, run, precision=prec, steps_per_graph=50)
         else:
@@ -304,6 +309,9 @@ def single_plate_bench(pkg, args):
         p.close()
     def rel(a, b):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    if len(precs) == 1:
+        print(json.dumps(out))
+        return
     out["fp32_vs_fp64_displ_rel_l2"] = rel(res[32]["displ"], res[64]["displ"])
     vel32 = np.diff(res[32]["displ"][1:], axis=0)
     vel64 = np.diff(res[64]["displ"][1:], axis=0)
@@ -370,6 +378,10 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="damage-gradient workload instead of the forward batch")
     ap.add_argument("--workload", choices=("batch", "force", "pzt", "solid", "wavefield"), default="batch",
                     help="batch: 512 plates (default); force: 20x20-element plate; pzt: 200x200 plate with PZT")
+    ap.add_argument("--nft", type=int, default=0,
+                    help="force/pzt/solid: stop the plate's run after this many steps (0 = the full run)")
+    ap.add_argument("--prec", type=int, default=0, choices=(0, 32, 64),
+                    help="force/pzt/solid: run one precision only (0 = FP64 and FP32, compared)")
     ap.add_argument("--adj-maps", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=20000)
     ap.add_argument("--plain-fp64", action="store_true",

@@ -2447,7 +2447,7 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
       double X[S_NPE][3];
       for (int c = 0; c < S_NPE; ++c) {
         const int nd = m.nodes[(int64_t)c * m.fen + e];
-        conn[(int64_t)c * FP + e0 + e] = (int)(n0 + nd - 1);
+        conn[(e0 + e) * S_NPE + c] = (int)(n0 + nd - 1);
         for (int b = 0; b < 3; ++b) X[c][b] = m.coords[(int64_t)b * m.nnode + nd - 1];
       }
       for (int c = 0; c < S_NPE; ++c) {
@@ -2475,9 +2475,8 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
         inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
         inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
         inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
-        const int64_t base = (int64_t)c * FP + e0 + e;
-        for (int q = 0; q < 9; ++q) geo[(int64_t)q * S_NPE * FP + base] = inv[q / 3][q % 3];
-        geo[(int64_t)9 * S_NPE * FP + base] = gw[cx] * gw[cy] * gw3[cz] * std::fabs(det);
+        for (int q = 0; q < 9; ++q) geo[((int64_t)q * FP + e0 + e) * S_NPE + c] = inv[q / 3][q % 3];
+        geo[((int64_t)9 * FP + e0 + e) * S_NPE + c] = gw[cx] * gw[cy] * gw3[cz] * std::fabs(det);
       }
     }
     std::vector<int> IG, IL;
@@ -2497,7 +2496,7 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
         const int e = (kl - 1) / S_NPE, c = (kl - 1) % S_NPE;
         const int64_t g = n0 + kg - 1;
         if (fillc[g] >= node_cnt[g]) return bad(p, "mesh: basket maps inconsistent with nodes");
-        slots[row_ptr[g] + fillc[g]++] = (int)(c * FP + e0 + e);
+        slots[row_ptr[g] + fillc[g]++] = (int)((e0 + e) * S_NPE + c);
       }
     for (int q = 0; q < runs[s].n_force; ++q) {
       const int d = runs[s].force_dof[q];
@@ -2528,8 +2527,8 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
     for (int q = row_ptr[g]; q < row_ptr[g + 1]; ++q) {
       const int64_t sl = slots[q];
       if (sl >= P0) continue;
-      const int64_t c = sl / FP, e = sl % FP;
-      mm += geo[(int64_t)9 * S_NPE * FP + c * FP + e] * erho[e];
+      const int64_t e = sl / S_NPE;
+      mm += geo[(int64_t)9 * FP * S_NPE + sl] * erho[e];
     }
     minv[g] = mm > 0 ? 1.0 / mm : 0.0;
     for (int f = 0; f < 3; ++f) p->mass[3 * g + f] = mm;
@@ -2539,7 +2538,7 @@ extern "C" shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh*
   std::vector<double> gbox((size_t)4 * FP, 0.0);
   bool box = true;
   for (int64_t e = 0; e < p->fen && box; ++e) {
-    auto G = [&](int q, int c) { return geo[((int64_t)q * S_NPE + c) * FP + e]; };
+    auto G = [&](int q, int c) { return geo[((int64_t)q * FP + e) * S_NPE + c]; };
     const double s0 = G(0, 0), s1 = G(4, 0), s2 = G(8, 0);
     const double v0 = G(9, 0) / (gw[0] * gw[0] * gw3[0]);
     const double scale = std::fabs(s0) + std::fabs(s1) + std::fabs(s2);

@@ -10,7 +10,9 @@
 // weighted fluxes staged in shared memory, the three 1D derivative matrices
 // (6-point along xi and eta, 3-point along zeta) applied by each thread along
 // its own node lines.  Element-local forces go to scratch and are assembled by
-// the node kernel exactly like the flat shell's general path.
+// the node kernel exactly like the flat shell's general path.  Per-element
+// arrays are element-major ([e][108]), so a CTA's threads (the nodes of its
+// elements) read and write consecutive words.
 #pragma once
 #include "shell_element.cuh"
 
@@ -39,9 +41,9 @@ template <typename T> struct SolidArgs {
   int nnode, fen, nn_first, nft;
   T* UA;
   T* UB;
-  T* F2;                           // [3][plane], element slots c*fen_pad + e, then force slots
-  const int* __restrict__ conn;    // [108][fen_pad]
-  const T* __restrict__ geo;       // [10][108][fen_pad]: invJ_ab (a = xi,eta,zeta; b = x,y,z) row-major, W
+  T* F2;                           // [3][plane], element slots e*108 + c, then force slots
+  const int* __restrict__ conn;    // [fen_pad][108]
+  const T* __restrict__ geo;       // [10][fen_pad][108]: invJ_ab (a = xi,eta,zeta; b = x,y,z) row-major, W
   const T* __restrict__ gbox;      // box elements: [4][fen_pad] dxi/dx, deta/dy, dzeta/dz, |det J|
   const int* __restrict__ emat;
   const T* __restrict__ ekeep;
@@ -74,6 +76,20 @@ template <typename T, bool kBox>
 __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int kstep) {
   __shared__ T su[S_EPB][3][S_NPE];
   __shared__ T sg[S_EPB][9][S_NPE];   // flux of field f along direction d at [f*3+d]
+  // D (6x6), D3 (3x3) and the GLL weights: each thread indexes them by its own
+  // node position, which the constant cache would serialise per distinct
+  // address; shared memory serves a warp's distinct addresses in one pass
+  __shared__ T sD[NP * NP + S_NZ * S_NZ + NP + S_NZ];
+  {
+    const int t = threadIdx.x;
+    if (t < NP * NP) sD[t] = Dm<T>(t / NP, t % NP);
+    else if (t < NP * NP + S_NZ * S_NZ) sD[t] = D3m<T>((t - NP * NP) / S_NZ, (t - NP * NP) % S_NZ);
+    else if (t < NP * NP + S_NZ * S_NZ + NP) sD[t] = Wg<T>(t - NP * NP - S_NZ * S_NZ);
+    else if (t < NP * NP + S_NZ * S_NZ + NP + S_NZ) sD[t] = W3m<T>(t - NP * NP - S_NZ * S_NZ - NP);
+  }
+  const T* sD3 = sD + NP * NP;
+  const T* sW = sD3 + S_NZ * S_NZ;
+  const T* sW3 = sW + NP;
   const int nn = *a.d_base + kstep;
   const T* __restrict__ cur = ((nn - a.nn_first) & 1) ? a.UB : a.UA;
   if (blockIdx.x == 0) {
@@ -91,7 +107,7 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
   const int c = threadIdx.x % S_NPE;
   const int e = blockIdx.x * S_EPB + le;
   const int cx = c % NP, cy = (c / NP) % NP, cz = c / (NP * NP);
-  const int node = a.conn[(int64_t)c * a.fen_pad + e];
+  const int node = a.conn[(int64_t)e * S_NPE + c];
 #pragma unroll
   for (int f = 0; f < 3; ++f) su[le][f][c] = cur[f * a.nnode_pad + node];
   __syncthreads();
@@ -102,11 +118,11 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
     T sx = T(0), sy = T(0), sz = T(0);
 #pragma unroll
     for (int m = 0; m < NP; ++m) {
-      sx = fma(Dm<T>(cx, m), su[le][f][cz * 36 + cy * NP + m], sx);
-      sy = fma(Dm<T>(cy, m), su[le][f][cz * 36 + m * NP + cx], sy);
+      sx = fma(sD[cx * NP + m], su[le][f][cz * 36 + cy * NP + m], sx);
+      sy = fma(sD[cy * NP + m], su[le][f][cz * 36 + m * NP + cx], sy);
     }
 #pragma unroll
-    for (int m = 0; m < S_NZ; ++m) sz = fma(D3m<T>(cz, m), su[le][f][m * 36 + cy * NP + cx], sz);
+    for (int m = 0; m < S_NZ; ++m) sz = fma(sD3[cz * S_NZ + m], su[le][f][m * 36 + cy * NP + cx], sz);
     d[f][0] = sx;
     d[f][1] = sy;
     d[f][2] = sz;
@@ -119,11 +135,11 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
     iJ[0][0] = a.gbox[e];
     iJ[1][1] = a.gbox[a.fen_pad + e];
     iJ[2][2] = a.gbox[2 * a.fen_pad + e];
-    W = Wg<T>(cx) * Wg<T>(cy) * W3m<T>(cz) * a.gbox[3 * a.fen_pad + e];
+    W = sW[cx] * sW[cy] * sW3[cz] * a.gbox[3 * a.fen_pad + e];
   } else {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * S_NPE + c) * a.fen_pad + e];
-    W = a.geo[((int64_t)9 * S_NPE + c) * a.fen_pad + e];
+    for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * a.fen_pad + e) * S_NPE + c];
+    W = a.geo[((int64_t)9 * a.fen_pad + e) * S_NPE + c];
   }
   // physical gradient g[f][b] = sum_a d[f][a] * invJ_ab  (strains_spec_p.m)
   T g[3][3];
@@ -163,12 +179,12 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
     T s = T(0);
 #pragma unroll
     for (int m = 0; m < NP; ++m) {
-      s = fma(Dm<T>(m, cx), sg[le][f * 3 + 0][cz * 36 + cy * NP + m], s);
-      s = fma(Dm<T>(m, cy), sg[le][f * 3 + 1][cz * 36 + m * NP + cx], s);
+      s = fma(sD[m * NP + cx], sg[le][f * 3 + 0][cz * 36 + cy * NP + m], s);
+      s = fma(sD[m * NP + cy], sg[le][f * 3 + 1][cz * 36 + m * NP + cx], s);
     }
 #pragma unroll
-    for (int m = 0; m < S_NZ; ++m) s = fma(D3m<T>(m, cz), sg[le][f * 3 + 2][m * 36 + cy * NP + cx], s);
-    a.F2[f * a.plane + (int64_t)c * a.fen_pad + e] = s;
+    for (int m = 0; m < S_NZ; ++m) s = fma(sD3[m * S_NZ + cz], sg[le][f * 3 + 2][m * 36 + cy * NP + cx], s);
+    a.F2[f * a.plane + (int64_t)e * S_NPE + c] = s;
   }
 }
 
