@@ -14,6 +14,8 @@
 // arrays are element-major ([e][108]), so a CTA's threads (the nodes of its
 // elements) read and write consecutive words.
 #pragma once
+#include <type_traits>
+
 #include "shell_element.cuh"
 
 namespace shm {
@@ -74,22 +76,45 @@ template <typename T> struct SolidArgs {
 // geometry values.
 template <typename T, bool kBox>
 __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int kstep) {
-  __shared__ T su[S_EPB][3][S_NPE];
-  __shared__ T sg[S_EPB][9][S_NPE];   // flux of field f along direction d at [f*3+d]
-  // D (6x6), D3 (3x3) and the GLL weights: each thread indexes them by its own
-  // node position, which the constant cache would serialise per distinct
-  // address; shared memory serves a warp's distinct addresses in one pass
-  __shared__ T sD[NP * NP + S_NZ * S_NZ + NP + S_NZ];
+  using T2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+  // node values in two orders: su[c] with c = cz*36 + cy*6 + cx (xi lines
+  // contiguous) and suT[cz*36 + cx*6 + cy] (eta lines contiguous), so that
+  // both 6-point contractions read pairs; fluxes along xi are kept in node
+  // order, fluxes along eta in eta-major order, for the same reason
+  __shared__ __align__(16) T su[S_EPB][3][S_NPE];
+  __shared__ __align__(16) T suT[S_EPB][3][S_NPE];
+  __shared__ __align__(16) T sg[S_EPB][9][S_NPE];   // flux of field f along direction d at [f*3+d]
+  // D and D' (6x6), D3 (3x3) and the GLL weights: each thread indexes them by
+  // its own node position, which the constant cache would serialise per
+  // distinct address; shared memory serves a warp's distinct addresses in one pass
+  constexpr int kTab = 2 * NP * NP + S_NZ * S_NZ + NP + S_NZ;
+  __shared__ __align__(16) T sD[kTab];
   {
     const int t = threadIdx.x;
-    if (t < NP * NP) sD[t] = Dm<T>(t / NP, t % NP);
-    else if (t < NP * NP + S_NZ * S_NZ) sD[t] = D3m<T>((t - NP * NP) / S_NZ, (t - NP * NP) % S_NZ);
-    else if (t < NP * NP + S_NZ * S_NZ + NP) sD[t] = Wg<T>(t - NP * NP - S_NZ * S_NZ);
-    else if (t < NP * NP + S_NZ * S_NZ + NP + S_NZ) sD[t] = W3m<T>(t - NP * NP - S_NZ * S_NZ - NP);
+    if (t < NP * NP) {
+      sD[t] = Dm<T>(t / NP, t % NP);
+      sD[NP * NP + t] = Dm<T>(t % NP, t / NP);
+    } else if (t < NP * NP + S_NZ * S_NZ) {
+      sD[NP * NP + t] = D3m<T>((t - NP * NP) / S_NZ, (t - NP * NP) % S_NZ);
+    } else if (t < NP * NP + S_NZ * S_NZ + NP) {
+      sD[NP * NP + t] = Wg<T>(t - NP * NP - S_NZ * S_NZ);
+    } else if (t < NP * NP + S_NZ * S_NZ + NP + S_NZ) {
+      sD[NP * NP + t] = W3m<T>(t - NP * NP - S_NZ * S_NZ - NP);
+    }
   }
-  const T* sD3 = sD + NP * NP;
+  const T* sDT = sD + NP * NP;     // sDT[i * NP + m] = D[m][i]
+  const T* sD3 = sDT + NP * NP;
   const T* sW = sD3 + S_NZ * S_NZ;
   const T* sW3 = sW + NP;
+  // six consecutive values from an even (16-byte aligned for FP64) index
+  auto ld6 = [](const T* p, T (&o)[NP]) {
+#pragma unroll
+    for (int k = 0; k < NP / 2; ++k) {
+      const T2 v = reinterpret_cast<const T2*>(p)[k];
+      o[2 * k] = v.x;
+      o[2 * k + 1] = v.y;
+    }
+  };
   const int nn = *a.d_base + kstep;
   const T* __restrict__ cur = ((nn - a.nn_first) & 1) ? a.UB : a.UA;
   if (blockIdx.x == 0) {
@@ -108,24 +133,37 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
   const int e = blockIdx.x * S_EPB + le;
   const int cx = c % NP, cy = (c / NP) % NP, cz = c / (NP * NP);
   const int node = a.conn[(int64_t)e * S_NPE + c];
+  const int cT = cz * 36 + cx * NP + cy;  // this node's eta-major index
 #pragma unroll
-  for (int f = 0; f < 3; ++f) su[le][f][c] = cur[f * a.nnode_pad + node];
+  for (int f = 0; f < 3; ++f) {
+    const T v = cur[f * a.nnode_pad + node];
+    su[le][f][c] = v;
+    suT[le][f][cT] = v;
+  }
   __syncthreads();
   // reference derivatives (Npx*U, Npy*U, Npz*U)
   T d[3][3];
+  {
+    T Dx[NP], Dy[NP];
+    ld6(sD + cx * NP, Dx);
+    ld6(sD + cy * NP, Dy);
 #pragma unroll
-  for (int f = 0; f < 3; ++f) {
-    T sx = T(0), sy = T(0), sz = T(0);
+    for (int f = 0; f < 3; ++f) {
+      T sx = T(0), sy = T(0), sz = T(0);
+      T ux[NP], uy[NP];
+      ld6(&su[le][f][cz * 36 + cy * NP], ux);
+      ld6(&suT[le][f][cz * 36 + cx * NP], uy);
 #pragma unroll
-    for (int m = 0; m < NP; ++m) {
-      sx = fma(sD[cx * NP + m], su[le][f][cz * 36 + cy * NP + m], sx);
-      sy = fma(sD[cy * NP + m], su[le][f][cz * 36 + m * NP + cx], sy);
+      for (int m = 0; m < NP; ++m) {
+        sx = fma(Dx[m], ux[m], sx);
+        sy = fma(Dy[m], uy[m], sy);
+      }
+#pragma unroll
+      for (int m = 0; m < S_NZ; ++m) sz = fma(sD3[cz * S_NZ + m], su[le][f][m * 36 + cy * NP + cx], sz);
+      d[f][0] = sx;
+      d[f][1] = sy;
+      d[f][2] = sz;
     }
-#pragma unroll
-    for (int m = 0; m < S_NZ; ++m) sz = fma(sD3[cz * S_NZ + m], su[le][f][m * 36 + cy * NP + cx], sz);
-    d[f][0] = sx;
-    d[f][1] = sy;
-    d[f][2] = sz;
   }
   T iJ[3][3];
   T W;
@@ -170,17 +208,23 @@ __global__ void __launch_bounds__(S_THREADS) k_elem_solid(SolidArgs<T> a, int ks
   for (int f = 0; f < 3; ++f)
 #pragma unroll
     for (int aa = 0; aa < 3; ++aa)
-      sg[le][f * 3 + aa][c] = kBox ? W * (S[f][aa] * iJ[aa][aa])
-                                   : W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
+      sg[le][f * 3 + aa][aa == 1 ? cT : c] =
+          kBox ? W * (S[f][aa] * iJ[aa][aa]) : W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
   __syncthreads();
   // transposed operators: Npx' (xi), Npy' (eta), Npz' (zeta)
+  T Tx[NP], Ty[NP];
+  ld6(sDT + cx * NP, Tx);
+  ld6(sDT + cy * NP, Ty);
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
     T s = T(0);
+    T gxi[NP], geta[NP];
+    ld6(&sg[le][f * 3 + 0][cz * 36 + cy * NP], gxi);
+    ld6(&sg[le][f * 3 + 1][cz * 36 + cx * NP], geta);
 #pragma unroll
     for (int m = 0; m < NP; ++m) {
-      s = fma(sD[m * NP + cx], sg[le][f * 3 + 0][cz * 36 + cy * NP + m], s);
-      s = fma(sD[m * NP + cy], sg[le][f * 3 + 1][cz * 36 + m * NP + cx], s);
+      s = fma(Tx[m], gxi[m], s);
+      s = fma(Ty[m], geta[m], s);
     }
 #pragma unroll
     for (int m = 0; m < S_NZ; ++m) s = fma(sD3[m * S_NZ + cz], sg[le][f * 3 + 2][m * 36 + cy * NP + cx], s);
