@@ -2,7 +2,7 @@
 
 Tolerances: FP64 paths <= 1e-10 relative L2 on signals and state (the only
 differences are summation order and the algebraically rearranged update);
-FP32 paths <= 1e-3 relative L2 on sensor signals (spec bound)."""
+FP32 paths <= 1e-3 relative L2 on sensor signals (the stated FP32 bound)."""
 import numpy as np
 import pytest
 
