@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; only
 ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
-it, and only as the checker (or as the timed CPU reference arm).
+it, and only as the test oracle (or as the timed CPU reference arm).
 
 Every function restates one file of the reference (paths are relative to the
 ma-shm repository) in the same arithmetic order, deliberately literal: loops

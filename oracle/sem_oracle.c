@@ -4,9 +4,10 @@
  *
  * TEST INFRASTRUCTURE ONLY.  The product never links, loads or calls this
  * file.  Parity unpinned: the reference has no golden outputs for this loop
- * (only its set-up constants are pinned, see tests/golden/).  tests/ use it as the checker, bench.py's --impl reference arm and
- * cpu_baseline leg time it as the reference's CPU path (the MATLAB original
- * cannot run without MATLAB).
+ * (only its set-up constants are pinned, see tests/golden/).  tests/ compare
+ * the GPU results with it; bench.py's --impl reference arm and cpu_baseline
+ * leg time it as the reference's CPU path (the MATLAB original cannot run
+ * without MATLAB).
  *
  * It follows src/models/flat_shell/flat_shell_engine/main_flat_shell.m,
  * MAIN LOOP (:651-920), literally, one element at a time:
