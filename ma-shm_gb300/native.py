@@ -9,8 +9,6 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-import numpy as np
-
 from . import build as _build
 
 SHM_OK, SHM_ERR_BAD_ARG, SHM_ERR_CUDA, SHM_ERR_DIVERGED, SHM_ERR_TIMEOUT, SHM_ERR_OOM, SHM_ERR_STATE, \
