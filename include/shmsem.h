@@ -188,8 +188,11 @@ shm_status shm_solid_plan_create(int32_t nscen, const shm_solid_mesh *meshes, co
  * d_e = 1 - elem_keep.  The forward pass keeps (u_n, u_{n-1}) every
  * `ckpt_every` steps, each segment is recomputed forward and the adjoint
  * lambda is stepped back through it with the same element operator; misfit
- * and gradient are accumulated in FP64.  Uses the general kernels.
- *   target [nscen][nft x n_out] column-major per scenario, like displ. */
+ * and gradient are accumulated in FP64.  Runs the plan's own kernels: the
+ * fused structured adjoint step on structured FP32 plans, the general element
+ * and node kernels otherwise.
+ *   target [nscen][nft x n_out] column-major per scenario, like displ;
+ *   misfit [nscen]; grad [total elements]. */
 shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *target, double *misfit,
                                 double *grad, int32_t ckpt_every, void *stream);
 /* Device time (ms, CUDA events) of the last shm_forward_backward's phases:
