@@ -263,6 +263,33 @@ def test_invalid_inputs_rejected(pkg):
         pkg.Plan(scs, run, path=2, precision=16)
 
 
+@pytest.mark.parametrize("path", [1, 2])
+def test_degenerate_runs(pkg, path):
+    """Runs the reference allows that do nothing: nft = 1 with the loop
+    starting at nn = 2 (no step: displ keeps its zero row), and a plate with
+    neither excitation nor outputs (the state stays exactly zero)."""
+    scs, run = small_case(pkg, nft_cap=40)
+    sc = scs[0]
+    one = pkg.RunConfig(dt=run.dt, nft=1, nn_first=2, eta_xy=run.eta_xy, eta_z=run.eta_z, h=run.h)
+    sc1 = pkg.Scenario(mesh=sc.mesh, mat_table=sc.mat_table, force_dof=sc.force_dof, force_val=sc.force_val,
+                       out_dof=sc.out_dof, signal=np.asarray(sc.signal)[:1])
+    quiet = pkg.Scenario(mesh=sc.mesh, mat_table=sc.mat_table, signal=sc.signal)
+    for prec in (64, 32):
+        plan = pkg.Plan([sc1], one, precision=prec, path=path)
+        out = plan.forward()[0]
+        U, Uo = plan.get_state()
+        plan.close()
+        assert out["displ"].shape == (1, len(sc.out_dof))
+        assert not out["displ"].any() and not U.any() and not Uo.any()
+        plan = pkg.Plan([quiet], run, precision=prec, path=path)
+        assert plan.info["path"] == path
+        out = plan.forward()[0]
+        U, Uo = plan.get_state()
+        plan.close()
+        assert out["displ"].shape == (run.nft, 0)
+        assert not U.any() and not Uo.any()
+
+
 def test_pzt_actuated_plate_matches_oracle(pkg):
     """PZT disc as actuator (equivalent loads) and sensor on a small plate:
     FP64 GPU (both paths) vs oracle on outputs, voltage and frames."""
