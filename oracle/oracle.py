@@ -251,8 +251,17 @@ class OracleSolid:
         mgL = np.repeat(self.W * np.repeat(rho_e, 108), 3)                           # mass3D_v2.m
         self.mg_raw = R.basket_scatter(mgL, self.Gd, self.Ld, self.ndof)
 
+    def apply_k(self, U):
+        """K U (3 DOF per node, reference DOF order) from one undamped,
+        unforced step of the loop started at u_n = u_{n-1} = U: the update gives
+        u_{n+1} = U - F / (a0 m), so F = a0 m (U - u_{n+1}); dt = 1 keeps the
+        step's force term dominant (no cancellation in U - u_{n+1})."""
+        U = np.asarray(U, float)
+        r = self.run(1.0, 2, np.zeros(2), nn_first=2, U0=U, uold0=U)
+        return self.mg_raw * (U - r["U"])
+
     def run(self, dt, nft, st, nn_first=2, eta_xy=0.0, eta_z=0.0, force_dof=(), force_val=(), out_dof=(),
-            nthreads=0):
+            nthreads=0, U0=None, uold0=None):
         a0, a1 = 1 / dt ** 2, 1 / (2 * dt)
         dv = np.zeros(self.ndof)
         dv[0::3] = eta_xy
@@ -290,8 +299,8 @@ class OracleSolid:
         displ = np.zeros(max(len(od), 1) * nft)
         A.nout, A.out_dof, A.displ = len(od), _p(od, I32P), _p(displ)
         A.nthreads = nthreads
-        U = np.zeros(self.ndof)
-        Uo = np.zeros(self.ndof)
+        U = np.zeros(self.ndof) if U0 is None else np.array(U0, float)
+        Uo = np.zeros(self.ndof) if uold0 is None else np.array(uold0, float)
         A.U, A.uold = _p(U), _p(Uo)
         lib = _load()
         lib.oracle_solid_run.restype = C.c_int
