@@ -263,6 +263,38 @@ def test_invalid_inputs_rejected(pkg):
         pkg.Plan(scs, run, path=2, precision=16)
 
 
+@pytest.mark.parametrize("path", [1, 2, 3])
+def test_rigid_body_fields_stay_at_rest(pkg, path):
+    """A plate at rest in a rigid-body field (u_n = u_{n-1} = r, no
+    excitation) stays in it on every kernel path: K r = 0 (translations, the
+    in-plane rotation u = -y, v = x, and the tilts w = x, phi_x = -1 and
+    w = y, phi_y = -1) and the damping term vanishes, so each step returns r
+    up to rounding."""
+    scs, run = small_case(pkg, nft_cap=200)
+    sc = scs[0]
+    quiet = pkg.Scenario(mesh=sc.mesh, mat_table=sc.mat_table, signal=np.zeros(run.nft))
+    x, y = sc.mesh["coords"][:, 0], sc.mesh["coords"][:, 1]
+    nn = x.size
+
+    def field(**comp):
+        U = np.zeros((nn, 5))
+        for k, v in comp.items():
+            U[:, "u phix v phiy w".split().index(k)] = v
+        return U.reshape(-1)
+    fields = [field(u=1e-3), field(v=1e-3), field(w=1e-3), field(u=-0.01 * y, v=0.01 * x),
+              field(w=0.01 * x, phix=-0.01), field(w=0.01 * y, phiy=-0.01)]
+    for prec, tol in ((64, 1e-10), (32, 1e-4)):
+        plan = pkg.Plan([quiet], run, precision=prec, path=path)
+        assert plan.info["path"] == min(path, 2)   # path 3: the structured kernel's generic template
+        for r in fields:
+            plan.set_state(r, r, run.nn_first)
+            plan.advance(150)
+            U, Uo = plan.get_state()
+            scale = np.abs(r).max()
+            assert np.abs(U - r).max() <= tol * scale and np.abs(Uo - r).max() <= tol * scale, (prec, path)
+        plan.close()
+
+
 @pytest.mark.parametrize("path", [1, 2])
 def test_degenerate_runs(pkg, path):
     """Runs the reference allows that do nothing: nft = 1 with the loop
