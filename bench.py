@@ -152,6 +152,26 @@ def rank_batch(W, plates, rank):
     return W.batch(n=plates, seed=1000 * rank)
 
 
+ARM_PARTS = {0xd0c: "Neoverse N1", 0xd40: "Neoverse V1", 0xd49: "Neoverse N2", 0xd4f: "Neoverse V2"}
+
+
+def cpu_model() -> str:
+    """The host CPU's name as /proc/cpuinfo gives it (x86 model name, or the
+    Arm implementer/part), for the CPU baseline's record."""
+    try:
+        info = open("/proc/cpuinfo").read()
+    except OSError:
+        return os.uname().machine
+    for line in info.splitlines():
+        if line.lower().startswith("model name"):
+            return line.split(":", 1)[1].strip()
+    part = [line.split(":", 1)[1].strip() for line in info.splitlines() if line.startswith("CPU part")]
+    if part:
+        code = int(part[0], 16)
+        return f"Arm {ARM_PARTS.get(code, hex(code))}"
+    return os.uname().machine
+
+
 def cpu_reference(scenarios, run, steps, nthreads=0, budget_s=20.0):
     """Oracle (FP64 port of the reference loop) on a bounded sample: the first
     plates of the batch, `steps` time steps each, all host threads."""
@@ -421,6 +441,7 @@ def main():
                "warmup": args.warmup, "ms_per_step": 1e3 * ndof / v, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
                "cpu_baseline": {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "cpu_model": cpu_model(),
                                 "sample": f"first {used} plates x {steps} time steps, FP64 oracle restating "
                                           "main_flat_shell.m:651-917, OpenMP over all host threads"},
                "e2e": {"value": v, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -487,6 +508,7 @@ def main():
         v, used, tt = cpu_reference(scs, run, 10, budget_s=15.0)
         v1, used1, tt1 = cpu_reference(scs[:2], run, 3, nthreads=1, budget_s=5.0)
         cpu = {"value": v, "unit": "DOF-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "cpu_model": cpu_model(),
                "sample": f"first {used} plates x 10 time steps ({tt:.1f} s), FP64 oracle, all host threads",
                "single_core_value": v1,
                "single_core_sample": f"first {used1} plates x 3 time steps ({tt1:.1f} s), one thread"}
