@@ -160,15 +160,15 @@ def cpu_model() -> str:
     Arm implementer/part), for the CPU baseline's record."""
     try:
         info = open("/proc/cpuinfo").read()
-    except OSError:
-        return os.uname().machine
-    for line in info.splitlines():
-        if line.lower().startswith("model name"):
-            return line.split(":", 1)[1].strip()
-    part = [line.split(":", 1)[1].strip() for line in info.splitlines() if line.startswith("CPU part")]
-    if part:
-        code = int(part[0], 16)
-        return f"Arm {ARM_PARTS.get(code, hex(code))}"
+        for line in info.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+        part = [line.split(":", 1)[1].strip() for line in info.splitlines() if line.startswith("CPU part")]
+        if part:
+            code = int(part[0], 16)
+            return f"Arm {ARM_PARTS.get(code, hex(code))}"
+    except (OSError, ValueError, IndexError):
+        pass
     return os.uname().machine
 
 
