@@ -7,7 +7,7 @@
  * pointers and sizes, MATLAB (column-major, 1-based) layouts at the boundary,
  * integer status codes, no exceptions, no CUDA or torch types.  A MEX gateway
  * (mexFunction) or a ctypes/cffi binding maps the solver's arguments onto
- * these calls; see INTEGRATION.md.
+ * these calls.
  *
  * Ownership: the caller owns every host array it passes; the plan copies what
  * it needs at creation and owns all device memory.  One plan is not
@@ -115,6 +115,8 @@ typedef struct {
 shm_status shm_plan_create(int32_t nscen, const shm_mesh *meshes, const shm_material *mats,
                            const shm_run *runs, const shm_options *opt, shm_plan **out);
 shm_status shm_plan_destroy(shm_plan *plan);
+/* Text of the plan's last error.  With plan == NULL: the text of the calling
+ * thread's last failed shm_stiffness_static call ("no plan" if none). */
 const char *shm_last_error(const shm_plan *plan);
 
 /* Whole forward solve, the MAIN LOOP (main_flat_shell.m:651-917).
@@ -126,6 +128,13 @@ const char *shm_last_error(const shm_plan *plan);
  * Any output pointer may be NULL.  `stream` is a cudaStream_t or NULL. */
 shm_status shm_forward(shm_plan *plan, const double *st, double *displ, double *voltage,
                        double *frames, void *stream);
+
+/* Blow-up guard interval.  The reference checks for a non-finite state or
+ * w > 10 h only at frame steps (main_flat_shell.m:786-804), so a run without
+ * frames is never checked; the engine also checks every `steps` time steps
+ * (default 100; 0 = at frame steps only).  A detected blow-up makes
+ * shm_advance / shm_forward return SHM_ERR_DIVERGED. */
+shm_status shm_set_guard_interval(shm_plan *plan, int32_t steps);
 
 /* Fine-grained stepping used by forward/adjoint drivers and benchmarks. */
 shm_status shm_reset(shm_plan *plan);                        /* zero state, nn = nn_first */
@@ -200,9 +209,12 @@ shm_status shm_forward_backward(shm_plan *plan, const double *st, const double *
 shm_status shm_forward_backward_timing(const shm_plan *plan, float *ms3);
 /* Device memory that shm_forward_backward may use to keep every state of the
  * last checkpoint segments of the forward pass (those segments are not
- * recomputed): max_bytes -1 = the device's spare memory less 8 GiB (default),
- * 0 = recompute every segment; values below -1 leave the setting unchanged.
- * last_segments (may be NULL) receives the number of segments the last call kept. */
+ * recomputed): max_bytes > 0 = at most that many bytes, 0 = recompute every
+ * segment, -3 = half of the device's free memory at the call (default),
+ * -1 = the device's free memory less 8 GiB (opt-in: leaves little to other
+ * users of the GPU, e.g. a MATLAB gpuArray pool); other negative values
+ * leave the setting unchanged.  last_segments (may be NULL) receives the
+ * number of segments the last call kept. */
 shm_status shm_set_adjoint_store(shm_plan *plan, int64_t max_bytes, int32_t *last_segments);
 
 /* Autotuner for plans on the structured path: times `steps` steps of the
@@ -234,8 +246,15 @@ shm_status shm_mass(shm_plan *plan, double *mg);
  * (SHM_STATIC_MAX_ELEMS elements, 5.9 MB, held by every GPU that loads the
  * library until exit); larger meshes return SHM_ERR_BAD_ARG.  The first call
  * on a device sets up that device (symbol address, constants): make it before
- * any stream capture.  All calls share the array, so calls that overlap on the
- * GPU race; calls ordered on one stream are safe.  FP64. */
+ * any stream capture.  The set-up is cached per device for the life of the
+ * process: a caller that resets the device (cudaDeviceReset) invalidates it,
+ * and the next call would use a stale address -- do not reset a device that
+ * this entry point has run on.  All calls share the array, so calls that
+ * overlap on the GPU race; calls ordered on one stream are safe (each call
+ * clears F and writes every element slot it reads).  Errors: SHM_ERR_BAD_ARG
+ * for sizes or NULL arrays, SHM_ERR_CUDA when a CUDA error was already pending
+ * (nothing is queued then) or a set-up step or launch fails;
+ * shm_last_error(NULL) names the step.  FP64. */
 #define SHM_STATIC_MAX_ELEMS 4096
 shm_status shm_stiffness_static(int32_t fen, int32_t nnode, const int32_t *nodes, const double *coords,
                                 const double *lam, int32_t basket_rows, const int32_t *I_G, const int32_t *I_L,

@@ -42,18 +42,39 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile libshmsem.so if any source is newer than the library."""
+    """Compile libshmsem.so if any source is newer than the library: each
+    translation unit in its own nvcc process (in parallel), then one link."""
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = LIB_PATH + ".tmp.%d" % os.getpid()
-    cmd = [nvcc(), *NVCC_FLAGS, "-I", os.path.join(REPO_DIR, "include"), "-o", tmp, *SOURCES]
-    if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
-    os.replace(tmp, LIB_PATH)
+    tag = ".tmp.%d" % os.getpid()
+    compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(BUILD_DIR, os.path.basename(src) + tag + ".o")
+        cmd = [nvcc(), *compile_flags, "-I", os.path.join(REPO_DIR, "include"), "-c", "-o", obj, src]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        objs.append(obj)
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+    errs = []
+    for p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            errs.append(out)
+    try:
+        if errs:
+            raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
+        tmp = LIB_PATH + tag
+        cmd = [nvcc(), "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp, *objs]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("nvcc link failed:\n" + res.stdout + res.stderr)
+        os.replace(tmp, LIB_PATH)
+    finally:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB_PATH
 
 

@@ -26,4 +26,8 @@ struct FramesView {
 };
 shm_status plan_frames_view(shm_plan* p, int scen, FramesView* v);
 
+// Text of the calling thread's last failed shm_stiffness_static call (NULL
+// when its last call succeeded or it made none).
+const char* static_last_error();
+
 }  // namespace shm

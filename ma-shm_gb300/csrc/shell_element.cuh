@@ -55,8 +55,16 @@ template <> __device__ __forceinline__ float Wg<float>(int r) { return c_w32[r];
 // first multiple of frm_int at or after the loop's first index.
 struct FrameSpec {
   int frm_int, nframes, nfields, fc0;
+  int guard_int;  // blow-up guard also every guard_int steps (0: at frame steps only)
   signed char slot[15];
 };
+
+// Steps at which the update checks for blow-up: the frame steps, as the
+// reference does (main_flat_shell.m:786-804), and every guard_int steps, so
+// that runs without frames are guarded too.
+__device__ __forceinline__ bool guard_step(const FrameSpec& fs, int nn) {
+  return (fs.frm_int > 0 && nn % fs.frm_int == 0) || (fs.guard_int > 0 && nn % fs.guard_int == 0);
+}
 
 template <typename T>
 __device__ __forceinline__ void store_frame(const FrameSpec& fs, T* __restrict__ frames, int64_t npad,

@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
   T* xs = sm + lane * ELEM_STRIDE;
   T* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
+  const bool guard = guard_step(a.fs, nn);
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false;
 
@@ -235,10 +236,8 @@ __global__ void __launch_bounds__(CTA_THREADS, sizeof(T) == 4 ? 3 : 1) k_struct_
           const T im = (f == 1 || f == 3) ? mr : mt;
           const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F);
           (a.outp ? a.outp : prev)[f * a.nnode_pad + node] = un;
-          if (frame) {
-            store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
-            if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
-          }
+          if (frame) store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
+          if (guard && (!isfinite(un) || (f == 4 && u > a.blowup))) bad = true;
         }
       }
       __syncthreads();

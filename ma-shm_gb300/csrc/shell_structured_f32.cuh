@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float* xs = sm + lane * ELEM_STRIDE;
   float* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
+  const bool guard = guard_step(a.fs, nn);
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false;
   // update prefetch: warp j finalises logical band row j of every lane group,
@@ -306,6 +307,9 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       ucol[gg] = min(OWN, t2.NX - ix0);
     }
+    int fcur[G];  // next force entry of each lane group's task (warp j's node rows)
+#pragma unroll
+    for (int gg = 0; gg < G; ++gg) fcur[gg] = pick<G>(gt, gg).f0;
 
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
     const unsigned colmask = ring_colmask<EW>(gt);
@@ -595,6 +599,31 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         // after the next CTA barrier.)
         __syncwarp();
       }
+      if constexpr (!kAdj) {
+        // excitation of this band row's owned nodes: the task's forces are
+        // ordered by node row (merged per DOF), warp j walks them with one
+        // cursor per lane group and its lanes subtract a row's entries from
+        // the completed band row (distinct DOFs: no two lanes meet)
+#pragma unroll
+        for (int gg = 0; gg < G; ++gg) {
+          const GroupTask& t2 = pick<G>(gt, gg);
+          if (t2.fn == 0 || !(r >= ulo[gg] && r < uhi[gg])) continue;
+          const int iy = 5 * (t2.eyA + r) + j;
+          const int fend = t2.f0 + t2.fn;
+          int c0 = fcur[gg];
+          while (c0 < fend && a.f_iy[c0] < iy) ++c0;
+          int c1 = c0;
+          while (c1 < fend && a.f_iy[c1] == iy) ++c1;
+          fcur[gg] = c1;
+          if (c1 > c0) {
+            const double sv = a.st[(int64_t)t2.scen * a.nft + (nn - 1)];
+            float* brow = band + gg * GM::FGS + prow * 5 * W;
+            for (int fi = c0 + lane; fi < c1; fi += 32)
+              brow[a.f_field[fi] * W + a.f_xl[fi]] -= (float)(a.f_val[fi] * sv);
+            __syncwarp();
+          }
+        }
+      }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
       if (kAdj && j == 0) {  // reduced after the next CTA barrier
         gpend = valid && owned_row && q > 0;
@@ -635,16 +664,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
               }
           }
           if (!kAdj && a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, node);
-          if (!kAdj && t2.fn > 0) {
-            const int iy = 5 * (t2.eyA + r) + j;
-            for (int fi = t2.f0; fi < t2.f0 + t2.fn; ++fi)
-              if (a.f_iy[fi] == iy && a.f_xl[fi] == 5 + c) {
-                const float fs = (float)(a.f_val[fi] * a.st[(int64_t)t2.scen * a.nft + (nn - 1)]);
-#pragma unroll
-                for (int f = 0; f < 5; ++f)
-                  if (f == a.f_field[fi]) F[f] -= fs;
-              }
-          }
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
             const float u = urow[f * W];
@@ -652,10 +671,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             const float im = (f == 1 || f == 3) ? mr_r[gg][s] : mt_r[gg][s];
             const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
             dst[f * a.nnode_pad + node] = un;
-            if (frame) {
-              store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
-              if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
-            }
+            if (frame) store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
+            if (guard && (!isfinite(un) || (f == 4 && u > a.blowup))) bad = true;
           }
         }
       // (the next row's first barrier separates this update from the ring

@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
   T* dst = a.outp ? a.outp : prev;
   const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
+  const bool guard = guard_step(a.fs, nn);
   bool bad = false;
 #pragma unroll
   for (int f = 0; f < 5; ++f) {
@@ -285,10 +286,8 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
     // u + k1*(u-uold) - k2*(F/M); F already contains -Fa*st(nn)
     const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
     dst[f * a.nnode_pad + g] = un;
-    if (frame) {
-      store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
-      if (!isfinite(un) || (f == 4 && u > a.blowup)) bad = true;
-    }
+    if (frame) store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
+    if (guard && (!isfinite(un) || (f == 4 && u > a.blowup))) bad = true;
   }
   if (bad) atomicOr(a.flag, 1);
 }
@@ -382,6 +381,7 @@ struct shm_plan {
   std::vector<int> out_off, sens_off, nout_s, nsens_s;
   int nout = 0, nsens = 0, nslot = 0, nforce = 0;
   int frm_int = 0, nframes = 0, nfields = 0;
+  int guard_int = 100;  // blow-up guard every guard_int steps besides the frame steps (0 = frame steps only)
   FrameSpec fspec{};
   std::vector<double> mass;  // [nnode][5] host copy (interleaved)
   // device memory
@@ -402,11 +402,13 @@ struct shm_plan {
   void *LA = nullptr, *LB = nullptr, *seg = nullptr, *ck = nullptr, *F2adj = nullptr;
   void* gbox = nullptr;  // 3D solid plans of axis-aligned box elements: [4][fen_pad]
   void* grect = nullptr; // flat-shell plans of axis-aligned rectangles: [3][fen_pad]
+  void *kt_U = nullptr, *kt_out = nullptr;  // shm_apply_stiffness: state in, assembled force out
+  int* kt_base = nullptr;
   cudaStream_t aux[2] = {nullptr, nullptr};  // adjoint: recompute and adjoint streams
   // explicit step states (adjoint recompute): cur/prev by parity, u_{n+1} into ov_out
   void *ov_UA = nullptr, *ov_UB = nullptr, *ov_out = nullptr;
   float fb_ms[3] = {0.f, 0.f, 0.f};  // last forward_backward: forward, recompute, adjoint (ms)
-  int64_t store_cap = -1;             // bytes for states kept by the forward pass (-1 = spare memory)
+  int64_t store_cap = -3;  // bytes for states kept by the forward pass (-1 spare memory, -3 half the free memory)
   // pressure loading: nodal frames [npf][nnode_pad], lumped areas, per-step weights
   int npf = 0;
   void *pf = nullptr, *parea = nullptr;
@@ -443,6 +445,7 @@ static shm_status bad(shm_plan* p, const std::string& m) {
 static shm_status set_frames(shm_plan* p, const shm_run& r, int ndof) {
   FrameSpec& fs = p->fspec;
   fs = FrameSpec{};
+  fs.guard_int = p->guard_int;
   for (int i = 0; i < 15; ++i) fs.slot[i] = -1;
   p->frm_int = r.frm_int > 0 ? r.frm_int : 0;
   p->nframes = p->nfields = 0;
@@ -820,6 +823,36 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     t.oiy.push_back(iy);
     t.ofield.push_back(sp.h_ofield[q]);
     t.oq.push_back(sp.h_oq[q]);
+  }
+  // each task's forces ordered by node row, then column and field, with the
+  // entries of one DOF merged (values summed in FP64): a step kernel walks them
+  // with one cursor per node row and scatters a row's entries in parallel
+  for (TaskTmp& t : tasks) {
+    const size_t n = t.fxl.size();
+    if (n == 0) continue;
+    std::vector<size_t> ord(n);
+    for (size_t i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+      if (t.fiy[a] != t.fiy[b]) return t.fiy[a] < t.fiy[b];
+      if (t.fxl[a] != t.fxl[b]) return t.fxl[a] < t.fxl[b];
+      return t.ffield[a] < t.ffield[b];
+    });
+    std::vector<int> xl, iy, fld;
+    std::vector<double> val;
+    for (size_t i : ord) {
+      if (!xl.empty() && xl.back() == t.fxl[i] && iy.back() == t.fiy[i] && fld.back() == t.ffield[i]) {
+        val.back() += t.fval[i];
+        continue;
+      }
+      xl.push_back(t.fxl[i]);
+      iy.push_back(t.fiy[i]);
+      fld.push_back(t.ffield[i]);
+      val.push_back(t.fval[i]);
+    }
+    t.fxl.swap(xl);
+    t.fiy.swap(iy);
+    t.ffield.swap(fld);
+    t.fval.swap(val);
   }
   // longest tasks first so that lane groups of a CTA stay in step
   std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
@@ -1559,7 +1592,11 @@ extern "C" shm_status shm_plan_destroy(shm_plan* p) {
   return SHM_OK;
 }
 
-extern "C" const char* shm_last_error(const shm_plan* p) { return p ? p->err.c_str() : "no plan"; }
+extern "C" const char* shm_last_error(const shm_plan* p) {
+  if (p) return p->err.c_str();
+  const char* s = shm::static_last_error();  // calls without a plan (shm_stiffness_static)
+  return s ? s : "no plan";
+}
 
 static cudaStream_t pick_stream(shm_plan* p, void* stream) {
   return stream ? (cudaStream_t)stream : p->stream;
@@ -1657,18 +1694,23 @@ extern "C" shm_status shm_advance(shm_plan* p, int32_t nsteps, void* stream) {
 extern "C" shm_status shm_time_steps(shm_plan* p, int32_t nsteps, float* ms) {
   if (!p || !ms) return SHM_ERR_BAD_ARG;
   cudaStream_t s = p->stream;
-  cudaEvent_t e0, e1;
-  CKP(p, cudaEventCreate(&e0));
-  CKP(p, cudaEventCreate(&e1));
-  CKP(p, cudaStreamSynchronize(s));
-  CKP(p, cudaEventRecord(e0, s));
-  shm_status st = advance_async(p, nsteps, s);
+  cudaEvent_t e[2] = {nullptr, nullptr};
+  auto timed = [&]() -> shm_status {
+    CKP(p, cudaEventCreate(&e[0]));
+    CKP(p, cudaEventCreate(&e[1]));
+    CKP(p, cudaStreamSynchronize(s));
+    CKP(p, cudaEventRecord(e[0], s));
+    shm_status st = advance_async(p, nsteps, s);
+    if (st != SHM_OK) return st;
+    CKP(p, cudaEventRecord(e[1], s));
+    CKP(p, cudaEventSynchronize(e[1]));
+    CKP(p, cudaEventElapsedTime(ms, e[0], e[1]));
+    return SHM_OK;
+  };
+  const shm_status st = timed();
+  for (cudaEvent_t ev : e)
+    if (ev) cudaEventDestroy(ev);  // released on every return path
   if (st != SHM_OK) return st;
-  CKP(p, cudaEventRecord(e1, s));
-  CKP(p, cudaEventSynchronize(e1));
-  CKP(p, cudaEventElapsedTime(ms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   return check_flag(p, s);
 }
 
@@ -1782,35 +1824,41 @@ extern "C" shm_status shm_set_state(shm_plan* p, const double* U, const double* 
 
 template <typename T>
 static shm_status apply_k_t(shm_plan* p, const double* U, double* F) {
-  // uses the general element kernel on a temporary copy, whatever the path
+  // uses the general element kernel on the plan's own stiffness buffers
+  // (allocated by the first call, released with the plan), whatever the path
   std::vector<T> h((size_t)5 * p->nnode_pad, T(0));
   for (int64_t g = 0; g < p->nnode; ++g)
     for (int f = 0; f < 5; ++f) h[(size_t)f * p->nnode_pad + g] = (T)U[5 * g + f];
-  T* dU = nullptr;
-  T* dOut = nullptr;
-  int* dbase = nullptr;
-  CKP(p, cudaMalloc(&dU, sizeof(T) * h.size()));
-  CKP(p, cudaMalloc(&dOut, sizeof(T) * h.size()));
-  CKP(p, cudaMalloc(&dbase, 4));
+  shm_status st;
+  if (!p->kt_U) {
+    T *u = nullptr, *o = nullptr;
+    int* b = nullptr;
+    if ((st = dalloc(p, &u, h.size())) != SHM_OK) return st;
+    if ((st = dalloc(p, &o, h.size())) != SHM_OK) return st;
+    if ((st = dalloc(p, &b, 1)) != SHM_OK) return st;
+    p->kt_U = u;
+    p->kt_out = o;
+    p->kt_base = b;
+  }
+  T* dU = (T*)p->kt_U;
+  T* dOut = (T*)p->kt_out;
   CKP(p, cudaMemcpy(dU, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
-  CKP(p, cudaMemcpy(dbase, &p->nn_first, 4, cudaMemcpyHostToDevice));
+  CKP(p, cudaMemcpy(p->kt_base, &p->nn_first, 4, cudaMemcpyHostToDevice));
   GenArgs<T> a = make_args<T>(p);
   a.UA = dU;
   a.UB = dU;
   a.nforce = 0;
   a.nout = 0;
-  a.d_base = dbase;
+  a.d_base = p->kt_base;
   const int nblk = (int)(p->fen_pad / CTA_ELEMS);
   k_elem_general<T, false><<<nblk, CTA_THREADS, elem_smem_bytes(sizeof(T) == 8 ? 64 : 32), p->stream>>>(a, 0);
+  CKP(p, cudaGetLastError());
   k_assemble_only<T><<<(int)((p->nnode + 255) / 256), 256, 0, p->stream>>>(a, dOut);
   CKP(p, cudaGetLastError());
   CKP(p, cudaMemcpyAsync(h.data(), dOut, sizeof(T) * h.size(), cudaMemcpyDeviceToHost, p->stream));
   CKP(p, cudaStreamSynchronize(p->stream));
   for (int64_t g = 0; g < p->nnode; ++g)
     for (int f = 0; f < 5; ++f) F[5 * g + f] = (double)h[(size_t)f * p->nnode_pad + g];
-  cudaFree(dU);
-  cudaFree(dOut);
-  cudaFree(dbase);
   return SHM_OK;
 }
 
@@ -1848,6 +1896,15 @@ static void drop_graph(shm_plan* p) {
     p->gexec = nullptr;
     p->gsteps = 0;
   }
+}
+
+extern "C" shm_status shm_set_guard_interval(shm_plan* p, int32_t steps) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (steps < 0) return bad(p, "guard interval must be >= 0");
+  p->guard_int = steps;
+  p->fspec.guard_int = steps;
+  drop_graph(p);  // the step kernels' arguments are captured by value
+  return SHM_OK;
 }
 
 extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out, int32_t* rows_out,
@@ -1981,8 +2038,10 @@ static shm_status fwd_bwd_t(shm_plan* p, const double* st, const double* target,
     if (p->store_cap >= 0) {
       nstore = (int)std::min<size_t>((size_t)nck, (size_t)p->store_cap / per);
     } else if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
-      const size_t margin = (size_t)8 << 30;
-      if (fr > margin + per) nstore = (int)std::min<size_t>((size_t)nck, (fr - margin) / per);
+      // -1: the device's spare memory less 8 GiB (opt-in); -3 (default): half
+      // of the free memory, leaving the rest to other users of the device
+      const size_t avail = p->store_cap == -1 ? (fr > ((size_t)8 << 30) ? fr - ((size_t)8 << 30) : 0) : fr / 2;
+      if (avail >= per) nstore = (int)std::min<size_t>((size_t)nck, avail / per);
     }
     while (nstore > 0 && cudaMalloc(&store, (size_t)nstore * k * SB) != cudaSuccess) {
       cudaGetLastError();
@@ -2205,7 +2264,7 @@ extern "C" shm_status shm_forward_backward_timing(const shm_plan* p, float* ms3)
 extern "C" shm_status shm_set_adjoint_store(shm_plan* p, int64_t max_bytes, int32_t* last_segments) {
   if (!p) return SHM_ERR_BAD_ARG;
   if (last_segments) *last_segments = p->last_nstore;
-  if (max_bytes >= -1) p->store_cap = max_bytes;
+  if (max_bytes >= -1 || max_bytes == -3) p->store_cap = max_bytes;
   return SHM_OK;
 }
 

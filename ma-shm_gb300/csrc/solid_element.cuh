@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
   }
   const T im = a.minv[g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
+  const bool guard = guard_step(a.fs, nn);
   bool bad = false;
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
@@ -255,10 +256,8 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
     const T uo = prev[f * a.nnode_pad + g];
     const T un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
     prev[f * a.nnode_pad + g] = un;
-    if (frame) {
-      store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
-      if (!isfinite(un)) bad = true;
-    }
+    if (frame) store_frame(a.fs, a.frames, a.nnode_pad, g, f, nn, u, uo, un, a.a0, a.a1);
+    if (guard && !isfinite(un)) bad = true;
   }
   if (bad) atomicOr(a.flag, 1);
 }

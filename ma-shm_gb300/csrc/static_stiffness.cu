@@ -30,7 +30,9 @@
 
 #include <cmath>
 #include <mutex>
+#include <string>
 
+#include "internal.h"
 #include "shmsem.h"
 #include "shell_element.cuh"
 
@@ -43,6 +45,15 @@ __device__ __align__(256) double g_static_f2[(size_t)5 * NPE * SHM_STATIC_MAX_EL
 constexpr int kMaxDevices = 64;
 double* s_f2_addr[kMaxDevices] = {nullptr};
 std::mutex s_setup_mutex;
+thread_local std::string t_err;  // text of this thread's last failed call
+
+// records which step failed; the error of a CUDA call made here is cleared so
+// that it does not surface in the caller's next error check
+shm_status fail(const char* stage, cudaError_t e, bool clear) {
+  if (clear) cudaGetLastError();
+  t_err = std::string("shm_stiffness_static: ") + stage + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? SHM_ERR_OOM : SHM_ERR_CUDA;
+}
 
 constexpr int kGeoStride = 4 * NPE + 1;  // X, Y, dX/dxi, dY/dxi per element (odd stride)
 
@@ -223,18 +234,24 @@ void gll6(double* D, double* w) {
 // once per device, with the device current
 shm_status setup_device(double** f2) {
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SHM_ERR_CUDA;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail("cudaGetDevice", e, true);
+  if (dev < 0 || dev >= kMaxDevices) {
+    t_err = "shm_stiffness_static: device ordinal beyond the library's table";
+    return SHM_ERR_CUDA;
+  }
   std::lock_guard<std::mutex> lock(s_setup_mutex);
   if (s_f2_addr[dev] == nullptr) {
     void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_static_f2) != cudaSuccess || ptr == nullptr) return SHM_ERR_CUDA;
+    if ((e = cudaGetSymbolAddress(&ptr, g_static_f2)) != cudaSuccess) return fail("cudaGetSymbolAddress", e, true);
+    if (ptr == nullptr) return fail("cudaGetSymbolAddress", cudaErrorInvalidSymbol, false);
     double D[NP * NP], w[NP];
     gll6(D, w);
-    if (cudaMemcpyToSymbol(c_D64, D, sizeof(D)) != cudaSuccess) return SHM_ERR_CUDA;
-    if (cudaMemcpyToSymbol(c_w64, w, sizeof(w)) != cudaSuccess) return SHM_ERR_CUDA;
-    if (cudaFuncSetAttribute(k_static_elem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)static_smem_bytes()) != cudaSuccess)
-      return SHM_ERR_CUDA;
+    if ((e = cudaMemcpyToSymbol(c_D64, D, sizeof(D))) != cudaSuccess) return fail("cudaMemcpyToSymbol", e, true);
+    if ((e = cudaMemcpyToSymbol(c_w64, w, sizeof(w))) != cudaSuccess) return fail("cudaMemcpyToSymbol", e, true);
+    if ((e = cudaFuncSetAttribute(k_static_elem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)static_smem_bytes())) != cudaSuccess)
+      return fail("cudaFuncSetAttribute", e, true);
     s_f2_addr[dev] = static_cast<double*>(ptr);
   }
   *f2 = s_f2_addr[dev];
@@ -246,17 +263,35 @@ shm_status setup_device(double** f2) {
 extern "C" shm_status shm_stiffness_static(int32_t fen, int32_t nnode, const int32_t* nodes, const double* coords,
                                            const double* lam, int32_t basket_rows, const int32_t* I_G,
                                            const int32_t* I_L, const double* U, double* F, void* stream) {
-  if (fen < 1 || fen > SHM_STATIC_MAX_ELEMS || nnode < 1 || basket_rows < 1) return SHM_ERR_BAD_ARG;
-  if (!nodes || !coords || !lam || !I_G || !I_L || !U || !F) return SHM_ERR_BAD_ARG;
+  if (fen < 1 || fen > SHM_STATIC_MAX_ELEMS || nnode < 1 || basket_rows < 1) {
+    t_err = "shm_stiffness_static: fen must be 1..SHM_STATIC_MAX_ELEMS, nnode and basket_rows >= 1";
+    return SHM_ERR_BAD_ARG;
+  }
+  if (!nodes || !coords || !lam || !I_G || !I_L || !U || !F) {
+    t_err = "shm_stiffness_static: NULL array";
+    return SHM_ERR_BAD_ARG;
+  }
+  // an error left pending by earlier work of the caller would be read back
+  // as a failed launch below: report it before anything is queued (and leave
+  // it pending for the caller's own check)
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return fail("a CUDA error was already pending, nothing queued", e, false);
   double* f2 = nullptr;
   shm_status st = setup_device(&f2);
   if (st != SHM_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (cudaMemsetAsync(F, 0, sizeof(double) * 5 * (size_t)nnode, s) != cudaSuccess) return SHM_ERR_CUDA;
+  if ((e = cudaMemsetAsync(F, 0, sizeof(double) * 5 * (size_t)nnode, s)) != cudaSuccess)
+    return fail("cudaMemsetAsync of F", e, true);
   const int nblk = (fen + CTA_ELEMS - 1) / CTA_ELEMS;
   k_static_elem<<<nblk, CTA_THREADS, static_smem_bytes(), s>>>(fen, nnode, nodes, coords, lam, U, f2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail("k_static_elem launch", e, false);
   const int tb = 256, nb = (basket_rows + tb - 1) / tb;
-  for (int b = 0; b < 12; ++b)
+  for (int b = 0; b < 12; ++b) {
     k_static_basket<<<nb, tb, 0, s>>>(basket_rows, b, nnode, fen * NPE, I_G, I_L, f2, F);
-  return cudaGetLastError() == cudaSuccess ? SHM_OK : SHM_ERR_CUDA;
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail("k_static_basket launch", e, false);
+  }
+  t_err.clear();
+  return SHM_OK;
 }
+
+const char* shm::static_last_error() { return t_err.empty() ? nullptr : t_err.c_str(); }

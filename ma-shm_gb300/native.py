@@ -15,6 +15,7 @@ SHM_OK, SHM_ERR_BAD_ARG, SHM_ERR_CUDA, SHM_ERR_DIVERGED, SHM_ERR_TIMEOUT, SHM_ER
     SHM_ERR_UNSUPPORTED = range(8)
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "DIVERGED", 4: "TIMEOUT", 5: "OOM", 6: "STATE",
                 7: "UNSUPPORTED"}
+SHM_STATIC_MAX_ELEMS = 4096   # element cap of shm_stiffness_static (include/shmsem.h)
 
 I32P = C.POINTER(C.c_int32)
 F64P = C.POINTER(C.c_double)
@@ -71,6 +72,7 @@ SIGNATURES = {
     "shm_plan_destroy": (C.c_int, [C.c_void_p]),
     "shm_last_error": (C.c_char_p, [C.c_void_p]),
     "shm_forward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_void_p]),
+    "shm_set_guard_interval": (C.c_int, [C.c_void_p, C.c_int32]),
     "shm_reset": (C.c_int, [C.c_void_p]),
     "shm_set_signal": (C.c_int, [C.c_void_p, F64P, C.c_void_p]),
     "shm_advance": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),

@@ -112,13 +112,19 @@ class Plan:
             e0 += fen
         return mis, out
 
-    def set_adjoint_store(self, max_bytes: int | None = None) -> int:
-        """Bytes forward_backward may keep for the last segments' states
-        (None: the device's spare memory; 0: recompute every segment).
-        Returns the number of segments the previous call kept."""
+    def set_guard_interval(self, steps: int):
+        """Blow-up guard every ``steps`` time steps besides the frame steps
+        (0: at frame steps only, as the reference)."""
+        self._check(self.lib.shm_set_guard_interval(self.handle, int(steps)))
+
+    def set_adjoint_store(self, max_bytes: int | str | None = None) -> int:
+        """Bytes forward_backward may keep for the last segments' states:
+        None = half of the device's free memory (the default), "spare" = the
+        free memory less 8 GiB, 0 = recompute every segment.  Returns the
+        number of segments the previous call kept."""
         n = C.c_int32()
-        self._check(self.lib.shm_set_adjoint_store(self.handle, -1 if max_bytes is None else int(max_bytes),
-                                                   C.byref(n)))
+        code = -3 if max_bytes is None else (-1 if max_bytes == "spare" else int(max_bytes))
+        self._check(self.lib.shm_set_adjoint_store(self.handle, code, C.byref(n)))
         return n.value
 
     def stored_segments(self) -> int:

@@ -6,9 +6,14 @@ Reads, as text, the constants the reference itself prints or hard-codes:
   * c3d_ref.json  <- src/models/common/engineering_2_C3D.m:1-24,42-51
                      (glass-epoxy engineering constants and the 3D stiffness
                      the reference prints in its comment, 1e10 Pa units)
-Run from the repository root:  python tests/golden/make_golden.py [REF_ROOT]
-REF_ROOT defaults to /root/reference.  The fixtures are committed; the tests
-never read the reference tree.
+  * homog_ref.json <- src/models/common/Homogenized_Cmatrix.m:1-7,27-37,54-58
+                     (fibre/matrix inputs, the printed shell q rows and the
+                     printed 3D stiffness row, 1e11 Pa units)
+  * damage_ref.json <- src/models/common/damage_model.m:10-16
+                     (the example 6x6 stiffness and damage degree in its comment)
+Run from the repository root:  python tests/golden/make_golden.py REF_ROOT
+where REF_ROOT is the reference checkout.  The fixtures are committed; the
+tests never read the reference tree.
 """
 from __future__ import annotations
 
@@ -70,8 +75,60 @@ def parse_c3d(path):
     return {"inputs": consts, "C_printed": rows, "scale": scale, "digits": 4}
 
 
+NUM = r"[-+]?\d+\.\d+(?:[eE][-+]?\d+)?"
+
+
+def parse_homogenized(path):
+    """Inputs (lines 1-7), the two printed shell rows [q11 q12 q22 q44 q55 q66]
+    and the printed 3D row [q11 q12 q13 q22 q23 q33 q44 q55 q66], all in
+    units of 1e11 Pa, and the printed density."""
+    txt = open(path).read()
+    inputs = {}
+    for name in ("rhom", "rhof", "em", "ef", "nim", "nif", "vol"):
+        m = re.search(r"^\s*" + name + r"\s*=\s*([0-9.eE+-]+)\s*;", txt, re.M)
+        inputs[name] = float(m.group(1))
+    lines = txt.splitlines()
+    i2 = next(i for i, ln in enumerate(lines) if ln.strip().startswith("[q11 q12 q22"))
+    i3 = next(i for i, ln in enumerate(lines) if ln.strip().startswith("[q11 q12 q13"))
+    shell_rows = []
+    for ln in lines[i2 + 1:i3]:
+        if ln.lstrip().startswith("%") and "=" not in ln:
+            nums = re.findall(NUM, ln)
+            if len(nums) == 6:
+                shell_rows.append([float(x) for x in nums])
+    rho = float(re.search(r"%\s*rho\s*=\s*(" + NUM + ")", txt).group(1))
+    solid = []
+    for ln in lines[i3 + 1:]:
+        if not ln.lstrip().startswith("%"):
+            break
+        if "1.0e+11" in ln:
+            continue
+        solid += [float(x) for x in re.findall(NUM, ln)]
+        if len(solid) >= 9:
+            break
+    return {"inputs": inputs, "shell_rows": shell_rows, "solid_row": solid[:9], "rho_printed": rho,
+            "scale": 1e11, "digits": 4}
+
+
+def parse_damage(path):
+    """The example stiffness C (6x6) and damage_degree of the comment block."""
+    txt = open(path).read()
+    d = float(re.search(r"%\s*damage_degree\s*=\s*([0-9.]+)\s*;", txt).group(1))
+    block = txt[txt.index("% C=["):]
+    rows = []
+    for ln in block.splitlines():
+        nums = re.findall(r"\d+\.\d+|\b0\b", ln)
+        if len(nums) == 6:
+            rows.append([float(x) for x in nums])
+        if len(rows) == 6:
+            break
+    return {"damage_degree": d, "C": rows}
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py REF_ROOT")
+    ref = sys.argv[1]
     g = parse_gll(os.path.join(ref, "src/models/flat_shell/flat_shell_engine/gll.m"))
     with open(os.path.join(HERE, "gll_ref.json"), "w") as f:
         json.dump({"source": "src/models/flat_shell/flat_shell_engine/gll.m:8-34",
@@ -80,7 +137,15 @@ def main():
     c["source"] = "src/models/common/engineering_2_C3D.m:5-24,42-51"
     with open(os.path.join(HERE, "c3d_ref.json"), "w") as f:
         json.dump(c, f, indent=1)
-    print("wrote", sorted(g), "and c3d_ref.json")
+    h = parse_homogenized(os.path.join(ref, "src/models/common/Homogenized_Cmatrix.m"))
+    h["source"] = "src/models/common/Homogenized_Cmatrix.m:1-7,27-37,54-58"
+    with open(os.path.join(HERE, "homog_ref.json"), "w") as f:
+        json.dump(h, f, indent=1)
+    dm = parse_damage(os.path.join(ref, "src/models/common/damage_model.m"))
+    dm["source"] = "src/models/common/damage_model.m:10-16"
+    with open(os.path.join(HERE, "damage_ref.json"), "w") as f:
+        json.dump(dm, f, indent=1)
+    print("wrote", sorted(g), "c3d_ref.json, homog_ref.json, damage_ref.json")
 
 
 if __name__ == "__main__":

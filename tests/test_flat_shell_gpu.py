@@ -251,6 +251,24 @@ def test_divergence_is_reported(pkg):
     plan.close()
 
 
+@pytest.mark.parametrize("path", [1, 2, 3])
+def test_divergence_without_frames_is_reported(pkg, path):
+    """The same blow-up in a run without frames (the benchmark's setting) is
+    caught by the periodic guard on every flat-shell kernel path; with the
+    guard at frame steps only (the reference's rule) it goes unreported."""
+    scs, run = small_case(pkg, nft_cap=400)
+    run.dt *= 6
+    assert run.frm_int == 0
+    plan = pkg.Plan(scs, run, precision=32, path=path, steps_per_graph=50)
+    with pytest.raises(pkg.native.ShmError) as ei:
+        plan.forward()
+    assert ei.value.status == pkg.native.SHM_ERR_DIVERGED
+    plan.set_guard_interval(0)
+    out = plan.forward()[0]          # the reference's rule: nothing checked, no error
+    assert not np.isfinite(out["displ"]).all() or np.abs(out["displ"]).max() > 10 * run.h
+    plan.close()
+
+
 def test_invalid_inputs_rejected(pkg):
     scs, run = small_case(pkg)
     sc = scs[0]

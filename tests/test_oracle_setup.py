@@ -64,6 +64,52 @@ def test_product_c3d_matches_oracle(pkg):
         np.testing.assert_allclose(M.degrade_c3d(Cp, d), R.damage_model(Co, d), rtol=1e-12, atol=1e-3)
 
 
+def _solid_c(row):
+    C = np.zeros((6, 6))
+    (C[0, 0], C[0, 1], C[0, 2], C[1, 1], C[1, 2], C[2, 2], C[3, 3], C[4, 4], C[5, 5]) = row
+    C[1, 0], C[2, 0], C[2, 1] = C[0, 1], C[0, 2], C[1, 2]
+    return C
+
+
+def test_homogenized_plate_stiffness_known_answer(pkg):
+    """Homogenized_Cmatrix.m prints, for one carbon/epoxy homogenisation, the
+    3D stiffness [q11 q12 q13 q22 q23 q33 q44 q55 q66] (:54-58) and the shell
+    stiffness [q11 q12 q22 q44 q55 q66] (:27-37, 1e11 Pa, 4 decimals).  The
+    function that produced them (homogenization.m) is not in the reference, so
+    the pin is the 3D -> shell reduction: the product's c3d_to_plate and the
+    oracle's C3D_2_C2D restatement take the printed 3D row to the printed
+    shell row whose q44 equals the 3D row's (the file's other shell row, from
+    an earlier run, has q44 = 0.0435 and no 3D counterpart: the file says
+    "something is wrong here").  The bound is 1e-4 (one printed digit)
+    because the inputs carry only four decimals; rho = rhom (1 - vol) +
+    rhof vol reproduces the printed density."""
+    g = json.load(open(os.path.join(GOLD, "homog_ref.json")))
+    C = _solid_c(np.array(g["solid_row"]) * g["scale"])
+    row = next(r for r in g["shell_rows"] if abs(r[3] - g["solid_row"][6]) < 1e-9)
+    qp = pkg.materials.c3d_to_plate(C)
+    got = np.array([qp[k] for k in ("q11", "q12", "q22", "q44", "q55", "q66")]) / g["scale"]
+    np.testing.assert_allclose(got, row, rtol=0, atol=1e-4)
+    np.testing.assert_allclose(np.array(R.c3d_2_c2d(C)) / g["scale"], row, rtol=0, atol=1e-4)
+    i = g["inputs"]
+    assert abs(i["rhom"] * (1 - i["vol"]) + i["rhof"] * i["vol"] - g["rho_printed"]) < 0.05
+
+
+def test_damage_model_on_reference_example(pkg):
+    """damage_model.m:10-16 gives an example stiffness and damage degree 0.5
+    (its result is not printed).  On that input the product's degrade_c3d
+    equals the oracle's restatement of :19-46, and the entries the formulas
+    scale directly come out as the formulas say: C33, C44, C55, C31, C32
+    halved, symmetry kept."""
+    g = json.load(open(os.path.join(GOLD, "damage_ref.json")))
+    C = np.array(g["C"])
+    d = g["damage_degree"]
+    got = pkg.materials.degrade_c3d(C, d)
+    np.testing.assert_allclose(got, R.damage_model(C, d), rtol=1e-15, atol=1e-14)
+    for (a, b) in ((2, 2), (3, 3), (4, 4), (2, 0), (2, 1)):
+        assert got[a, b] == pytest.approx((1 - d) * C[a, b], rel=1e-15)
+    np.testing.assert_array_equal(got, got.T)
+
+
 def test_shape_derivatives_match_product_d(pkg):
     """shape2D_prim.m blocks = I (x) D and D (x) I with the product's D."""
     x, _ = R.gll(6)
