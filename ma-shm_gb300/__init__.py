@@ -10,7 +10,7 @@ The directory name contains a hyphen; import it through
 ``__graft_entry__.package()`` (it registers the module as ``mashm_gb300``).
 """
 from . import build, element, materials, mesh, mesher, native, pzt, solver, wavefield, workloads  # noqa: F401
-from .solver import Plan, RunConfig, Scenario, SolidPlan, SolidScenario, hanning_signal, main_flat_shell, random_signal  # noqa: F401
+from .solver import Plan, RunConfig, Scenario, SolidPlan, SolidScenario, hanning_signal, main_flat_shell, main_flat_shell_multi_pzt_c, random_signal  # noqa: F401
 
-__all__ = ["Plan", "RunConfig", "Scenario", "hanning_signal", "main_flat_shell", "build", "element", "materials", "workloads",
+__all__ = ["Plan", "RunConfig", "Scenario", "hanning_signal", "main_flat_shell", "main_flat_shell_multi_pzt_c", "build", "element", "materials", "workloads",
            "mesh", "native", "solver", "wavefield"]

@@ -1,9 +1,11 @@
 """Host side of the engine: plans, scenarios and the reference's solver entry point.
 
-``main_flat_shell`` mirrors the reference's
+``main_flat_shell`` and ``main_flat_shell_multi_pzt_c`` mirror the reference's
 ``t_frames = main_flat_shell(test_case, input_no, meshfile, mode, output_name, tasks)``
-(src/models/flat_shell/flat_shell_engine/main_flat_shell.m:1) and its output
-layout (displ<N>.mat, voltage<N>.mat, time<N>.mat, V?_frame<c>.mat).  The time
+(src/models/flat_shell/flat_shell_engine/main_flat_shell.m:1) and
+``main_flat_shell_multi_pzt_c(actuator_no, ...)`` (main_flat_shell_multi_pzt_c.m:1)
+with their output layout (displ<N>.mat, voltage<N>.mat for PZT plates,
+time<N>.mat, {U,V,A}?_frame<c>.mat).  The time
 loop itself runs in libshmsem.so on the GPU; this module only prepares inputs
 and writes results.  There is no CPU path: ``mode`` other than 'gpu' raises.
 """
@@ -379,27 +381,131 @@ def random_signal(nft: int, seed: int = 0) -> np.ndarray:
     return np.random.default_rng(seed).standard_normal(nft)
 
 
+def _laminate(inputs):
+    """Laminate of an input file: a material table row (``mat_table``, with
+    ply thicknesses ``lh``) or the ply constants q11..q66, rho, lh, lalpha of
+    the _c variants (composite_plate_c_delam_pzt.m).  Returns (laminate dict
+    or None, table [nmat, 23], total thickness h)."""
+    from . import materials as M
+    if "mat_table" in inputs:
+        return None, np.atleast_2d(inputs["mat_table"]), float(np.sum(inputs["lh"]))
+    q = {k: inputs[k] for k in ("q11", "q12", "q22", "q44", "q55", "q66")}
+    lam = M.laminate(q, inputs["rho"], inputs["lh"], inputs["lalpha"])
+    return lam, table_row(lam)[None, :], lam["h"]
+
+
+def _pzt_elements(mesh):
+    """PZT element lists of a mesh file, 0-based: ``pztEl`` as a cell array
+    (a list of 1-based element vectors, main_flat_shell_multi_pzt_c.m:47-50)
+    or as a matrix with one PZT per row (main_flat_shell.m:128-136)."""
+    pe = mesh.get("pztEl")
+    if pe is None:
+        return []
+    if isinstance(pe, np.ndarray) and pe.dtype != object and pe.ndim == 2:
+        rows = [r for r in pe]
+    elif isinstance(pe, np.ndarray) and pe.dtype != object:
+        rows = [pe] if pe.size else []
+    else:
+        rows = list(pe)
+    return [np.asarray(r, np.int64).ravel() - 1 for r in rows if np.asarray(r).size]
+
+
+def _pzt_plate(inputs, mesh, lam, h, pzt_elems, actuator):
+    """Bonded PZTs (all elements of every PZT carry the piezo layer,
+    composite_plate_c_delam_pzt.m) and the equivalent loads of PZT
+    ``actuator`` driven at V0 (main_flat_shell.m:144-225).  Returns
+    (table, elem_mat, force_dof, force_val, pzt constants)."""
+    from . import materials as M
+    from . import pzt as PZ
+    if lam is None:
+        raise ValueError("PZT plates need the ply constants q11..q66, rho, lh, lalpha (not a material table)")
+    pm = M.pzt_material(np.asarray(inputs["Spzt"], float), np.asarray(inputs["dp"], float),
+                        np.asarray(inputs["epsT"], float), float(inputs.get("theta_pzt", 0.0)))
+    t_pzt = float(inputs["pzt_thickness"])
+    lam_p = M.add_piezo_layer(lam, pm["Qpzt"], float(inputs["rho_pzt"]), t_pzt)
+    fen = np.asarray(mesh["nodes"]).shape[0]
+    elem_mat = np.zeros(fen, np.int32)
+    for e in pzt_elems:
+        elem_mat[e] = 1
+    Fa = PZ.actuator_loads(mesh, pzt_elems[actuator], t_pzt, h, float(inputs["V0"]), pm["epzt"], pm["gpzt"])
+    nzi = np.nonzero(Fa)[0]
+    table = np.stack([table_row(lam), table_row(lam_p)])
+    pzt = dict(pzt_thickness=t_pzt, g33=pm["g33"], e31=pm["e31"], e32=pm["e32"])
+    return table, elem_mat, (nzi + 1).astype(np.int32), Fa[nzi], pzt
+
+
+def _frame_interval(inputs, nft):
+    """frm_int of the input file: floor(nft/nFrames) for an even nft, the
+    input's own frm_int for an odd one (main_flat_shell_multi_pzt_c.m:37-43)."""
+    nframes = int(inputs.get("nFrames", 0))
+    if not nframes:
+        return 0, 0
+    if nft % 2 and "frm_int" in inputs:
+        return nframes, int(inputs["frm_int"])
+    return nframes, nft // nframes
+
+
+def _solve_and_write(sc, run, test_case, output_name, precision, t, nframes, fv, total_nodes, with_voltage):
+    """Runs the plan and writes the reference's files: displ<N>.mat,
+    voltage<N>.mat (PZT sensors), time<N>.mat (minTime, averageTime,
+    TotalNofNodes, t) and the frame files; returns t_frames."""
+    from scipy.io import savemat
+    os.makedirs(output_name, exist_ok=True)
+    nft, frm_int, nn_first = run.nft, run.frm_int, run.nn_first
+    tic = time.perf_counter()
+    plan = Plan([sc], run, precision=precision)
+    try:
+        res = plan.forward(want_frames=frm_int > 0)[0]
+    finally:
+        plan.close()
+    elapsed = time.perf_counter() - tic
+    if with_voltage:
+        savemat(os.path.join(output_name, f"voltage{test_case}.mat"), {"voltage": res["voltage"]})
+    savemat(os.path.join(output_name, f"displ{test_case}.mat"), {"displ": res["displ"]})
+    # minTime is the fastest step in the reference (tic/toc per step); the
+    # engine runs the loop as one device job, so both are the mean step time
+    savemat(os.path.join(output_name, f"time{test_case}.mat"),
+            {"minTime": elapsed / max(nft - 1, 1), "averageTime": elapsed / max(nft - 1, 1),
+             "TotalNofNodes": total_nodes, "t": t})
+    t_frames = np.zeros(nframes)
+    if "frames" in res:
+        names = [p + c for p in {"displacement": "U", "velocity": "V", "acceleration": "A",
+                                 "all": "UVA"}[fv] for c in ("x", "Fix", "y", "Fiy", "z")]
+        first = (nn_first + frm_int - 1) // frm_int
+        for c in range(min(res["frames"].shape[0], nframes)):
+            t_frames[c] = t[(c + first) * frm_int - 1]
+            for name, fld in zip(names, res["frames"][c]):
+                savemat(os.path.join(output_name, f"{name}_frame{c + 1}.mat"), {name: fld[:, None]})
+    return t_frames
+
+
+_KINDS = {"velocity": 0, "displacement": 1, "acceleration": 2, "all": 3}
+
+
 def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", output_name: str = ".",
                     tasks=(), precision: int = 64, variant: str = "main_flat_shell"):
     """Flat-shell forward solve with the reference's interface and outputs.
 
     inputs: the fields of an ``inputs/input<N>.m`` script (nft, tt, f_1, f_2,
-    t_1, nFrames, field_variable, etad_xy, etad_z, V0, lh, and the laminate as
-    a material table ``mat_table`` or q11..q66 + lalpha + rho).
+    t_1, nFrames, field_variable, etad_xy, etad_z, V0, and the laminate as a
+    material table ``mat_table`` with ``lh`` or q11..q66 + rho + lh + lalpha;
+    for a PZT plate also Spzt, dp, epsT, theta_pzt, rho_pzt, pzt_thickness).
     mesh:   the fields of the mesh .mat file (nodes, coords, optional I_G, I_L,
-    mesh_min, mesh_max, nex/ney for structured plates).
-    variant: 'main_flat_shell' (dt = tt/nft, loop nn = 2..nft, force at the
-    plate centre) or 'force_excit_c' (dt = tt/(nft-1), nn = 1..nft, force at
-    ``force_coords``, outputs at ``output_coords``).
-    Writes displ<test_case>.mat, time<test_case>.mat and the wavefield frames
-    {U,V,A}{x,Fix,y,Fiy,z}_frame<c>.mat of field_variable 'displacement',
-    'velocity', 'acceleration' or 'all' (main_flat_shell.m:806-885) into
-    output_name; returns t_frames.
+    mesh_min, mesh_max, nex/ney for structured plates, pztEl).
+    variant: 'main_flat_shell' (dt = tt/nft, loop nn = 2..nft, output and
+    force at the node nearest (mesh_max - mesh_min)/2; with ``pztEl`` the
+    first PZT is actuator and sensor instead of the point force,
+    main_flat_shell.m:121-225) or 'force_excit_c' (dt = tt/(nft-1),
+    nn = 1..nft, force at ``force_coords``, outputs at ``output_coords``).
+    Writes displ<test_case>.mat, voltage<test_case>.mat (PZT plates,
+    main_flat_shell.m:925), time<test_case>.mat with TotalNofNodes = dof/3 as
+    main_flat_shell.m:929 computes it (the 'force_excit_c' variant: dof/5)
+    and the wavefield frames {U,V,A}{x,Fix,y,Fiy,z}_frame<c>.mat of
+    field_variable 'displacement', 'velocity', 'acceleration' or 'all'
+    (main_flat_shell.m:806-885) into output_name; returns t_frames.
     """
     if mode != "gpu":
         raise ValueError("this engine runs the time loop on the GPU only (mode='gpu')")
-    from scipy.io import savemat
-    from . import materials as M
     from . import mesh as MS
 
     nft = int(inputs["nft"])
@@ -408,14 +514,7 @@ def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", outp
     else:
         dt, nn_first = inputs["tt"] / (nft - 1), 1
     t, st = hanning_signal(dt, nft, inputs["f_1"], inputs["f_2"], inputs.get("t_1", 0.0))
-    if "mat_table" in inputs:
-        table = np.atleast_2d(inputs["mat_table"])
-        h = float(np.sum(inputs["lh"]))
-    else:
-        q = {k: inputs[k] for k in ("q11", "q12", "q22", "q44", "q55", "q66")}
-        lam = M.laminate(q, inputs["rho"], inputs["lh"], inputs["lalpha"])
-        table = table_row(lam)[None, :]
-        h = lam["h"]
+    lam, table, h = _laminate(inputs)
     coords = np.asarray(mesh["coords"], float)
     if variant == "main_flat_shell":
         cen = (np.asarray(mesh["mesh_max"]) - np.asarray(mesh["mesh_min"])) / 2
@@ -428,33 +527,62 @@ def main_flat_shell(test_case, inputs: dict, mesh: dict, mode: str = "gpu", outp
     nframes = int(inputs.get("nFrames", 0))
     frm_int = nft // nframes if nframes else 0
     fv = inputs.get("field_variable", "velocity")
-    sc = Scenario(mesh=mesh, mat_table=table, force_dof=np.array([5 * force_node], np.int32),
-                  force_val=np.array([inputs["V0"]]), out_dof=5 * np.array(out_nodes, np.int32), signal=st)
-    kinds = {"velocity": 0, "displacement": 1, "acceleration": 2, "all": 3}
-    if fv not in kinds:
-        raise ValueError(f"field_variable must be one of {sorted(kinds)}")
+    if fv not in _KINDS:
+        raise ValueError(f"field_variable must be one of {sorted(_KINDS)}")
+    pzts = _pzt_elements(mesh) if variant == "main_flat_shell" else []
+    if pzts:
+        table, elem_mat, fdof, fval, pzt = _pzt_plate(inputs, mesh, lam, h, pzts[:1], 0)
+        sc = Scenario(mesh=mesh, mat_table=table, elem_mat=elem_mat, force_dof=fdof, force_val=fval,
+                      out_dof=5 * np.array(out_nodes, np.int32), signal=st, sensors=[pzts[0]], pzt=pzt)
+    else:
+        sc = Scenario(mesh=mesh, mat_table=table, force_dof=np.array([5 * force_node], np.int32),
+                      force_val=np.array([inputs["V0"]]), out_dof=5 * np.array(out_nodes, np.int32), signal=st)
     run = RunConfig(dt=dt, nft=nft, nn_first=nn_first, eta_xy=inputs.get("etad_xy", 0.0),
-                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int, frame_dof=0, frame_kind=kinds[fv])
-    os.makedirs(output_name, exist_ok=True)
-    tic = time.perf_counter()
-    plan = Plan([sc], run, precision=precision)
-    try:
-        res = plan.forward(want_frames=frm_int > 0)[0]
-    finally:
-        plan.close()
-    elapsed = time.perf_counter() - tic
-    savemat(os.path.join(output_name, f"displ{test_case}.mat"), {"displ": res["displ"]})
-    n_nodes = coords.shape[0]
-    savemat(os.path.join(output_name, f"time{test_case}.mat"),
-            {"minTime": elapsed / max(nft - 1, 1), "averageTime": elapsed / max(nft - 1, 1),
-             "TotalNofNodes": n_nodes, "t": t})
-    t_frames = np.zeros(nframes)
-    if "frames" in res:
-        names = [p + c for p in {"displacement": "U", "velocity": "V", "acceleration": "A",
-                                 "all": "UVA"}[fv] for c in ("x", "Fix", "y", "Fiy", "z")]
-        first = (nn_first + frm_int - 1) // frm_int
-        for c in range(min(res["frames"].shape[0], nframes)):
-            t_frames[c] = t[(c + first) * frm_int - 1]
-            for name, fld in zip(names, res["frames"][c]):
-                savemat(os.path.join(output_name, f"{name}_frame{c + 1}.mat"), {name: fld[:, None]})
-    return t_frames
+                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int, frame_dof=0, frame_kind=_KINDS[fv])
+    dof = 5 * coords.shape[0]
+    total = dof / 3 if variant == "main_flat_shell" else dof / 5
+    return _solve_and_write(sc, run, test_case, output_name, precision, t, nframes, fv, total, bool(pzts))
+
+
+def main_flat_shell_multi_pzt_c(actuator_no, test_case, inputs: dict, mesh: dict, mode: str = "gpu",
+                                output_name: str = ".", tasks=(), precision: int = 64):
+    """The reference's benchmarked solver entry point
+    ``t_frames = main_flat_shell_multi_pzt_c(actuator_no, test_case, input_no,
+    meshfile, mode, output_name, tasks)``
+    (src/models/flat_shell/flat_shell_engine/main_flat_shell_multi_pzt_c.m:1).
+
+    Every PZT of the mesh (``pztEl``: a list of 1-based element vectors) is
+    bonded (piezo layer in its elements, composite_plate_c_delam_pzt.m) and
+    is a sensor; PZT ``actuator_no`` (1-based) is driven at V0 by the Hann
+    burst (:150-230).  dt = tt/(nft-1), loop nn = 1..nft (:154,577); the
+    output is w at the node nearest (mesh_max - mesh_min)/2 (:57-60).
+    Writes voltage<test_case>.mat [nft x nPZT], displ<test_case>.mat,
+    time<test_case>.mat with TotalNofNodes = dof/5 (:860-861) and the frame
+    files of field_variable (:696-835) into output_name; returns t_frames.
+    inputs as for ``main_flat_shell`` (ply constants and PZT constants
+    required)."""
+    if mode != "gpu":
+        raise ValueError("this engine runs the time loop on the GPU only (mode='gpu')")
+    from . import mesh as MS
+
+    nft = int(inputs["nft"])
+    dt = inputs["tt"] / (nft - 1)
+    t, st = hanning_signal(dt, nft, inputs["f_1"], inputs["f_2"], inputs.get("t_1", 0.0))
+    lam, _, h = _laminate(inputs)
+    pzts = _pzt_elements(mesh)
+    if not 1 <= int(actuator_no) <= len(pzts):
+        raise ValueError(f"actuator_no must be 1..{len(pzts)} (the mesh's pztEl)")
+    table, elem_mat, fdof, fval, pzt = _pzt_plate(inputs, mesh, lam, h, pzts, int(actuator_no) - 1)
+    coords = np.asarray(mesh["coords"], float)
+    cen = (np.asarray(mesh["mesh_max"]) - np.asarray(mesh["mesh_min"])) / 2
+    out_node = MS.nearest_node(coords, cen[0], cen[1])
+    nframes, frm_int = _frame_interval(inputs, nft)
+    fv = inputs.get("field_variable", "velocity")
+    if fv not in _KINDS:
+        raise ValueError(f"field_variable must be one of {sorted(_KINDS)}")
+    sc = Scenario(mesh=mesh, mat_table=table, elem_mat=elem_mat, force_dof=fdof, force_val=fval,
+                  out_dof=np.array([5 * out_node], np.int32), signal=st, sensors=pzts, pzt=pzt)
+    run = RunConfig(dt=dt, nft=nft, nn_first=1, eta_xy=inputs.get("etad_xy", 0.0),
+                    eta_z=inputs.get("etad_z", 0.0), h=h, frm_int=frm_int, frame_dof=0, frame_kind=_KINDS[fv])
+    dof = 5 * coords.shape[0]
+    return _solve_and_write(sc, run, test_case, output_name, precision, t, nframes, fv, dof / 5, True)
