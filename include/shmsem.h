@@ -219,9 +219,10 @@ shm_status shm_set_adjoint_store(shm_plan *plan, int64_t max_bytes, int32_t *las
 
 /* Autotuner for plans on the structured path: times `steps` steps of the
  * general kernels and of every (elements per lane group, element rows per
- * task) candidate of the structured kernel -- {16, 32} x {4, 8, 16, 32, 64} --
- * re-planning the task list each time, keeps the fastest and resets the
- * state.  Returns the choice (tile_elems = 0: general kernels) and its ms per
+ * task) candidate of the structured kernel -- {16, 32} x {4, 8, 16, 32, 64,
+ * and per width the fewest rows that keep all tasks within one and within
+ * two waves of two CTAs per SM} -- re-planning the task list each time, keeps
+ * the fastest and resets the state.  Returns the choice (tile_elems = 0: general kernels) and its ms per
  * step. */
 shm_status shm_autotune(shm_plan *plan, int32_t steps, int32_t *tile_elems, int32_t *rows_per_block,
                         float *ms_per_step);

@@ -4,17 +4,22 @@
 // element columns swept bottom to top, shared-memory force band, every node
 // owned by one task), restructured for throughput:
 //  * u_n of the strip lives in a shared-memory ring of 11 node rows; the 5 new
-//    node rows of the next element row are copied with cp.async while the
-//    current row is computed, so the gather never waits on memory;
+//    node rows of the next element row arrive by TMA bulk copies
+//    (cp.async.bulk, one per node row and field, completed on an mbarrier)
+//    while the current row is computed, so the gather never waits on memory;
+//  * the update's operands of the row (u_{n-1} and the inverse mass of the
+//    node rows it completes) are bulk-copied into shared memory at the row's
+//    start, so their DRAM latency hides behind the row's element work;
 //  * the 6x6 contractions, resultants and fluxes run on packed FP32x2 FMA
 //    (__ffma2_rn, two lanes of a 64-bit register pair per instruction);
 //  * the force band is a 6-row ring (the shared node row is carried by
-//    re-labelling, not copied);
-//  * the update's loads of u_{n-1} and 1/M are issued before phase C so that
-//    their latency overlaps the transposed operator;
-//  * the laminate pairs are copied with cp.async one row ahead
-//    (double-buffered); the material index is read two rows ahead and the
-//    stiffness factor one row ahead into registers.
+//    re-labelling, not copied); the column part of the transposed operator is
+//    written into it directly (phase B), the row part added on top (phase C);
+//  * the laminate pairs of the next row are copied with cp.async after the
+//    last read of the current row's; the material index is read two rows
+//    ahead and the stiffness factor one row ahead into registers.
+// Every bulk copy starts and ends on a 16-byte boundary: it covers the needed
+// columns rounded out to 4 floats, and a per-row offset locates column 0.
 // Results equal the generic kernel's up to FP32 rounding order.
 #pragma once
 #include <cuda_fp16.h>
@@ -44,29 +49,94 @@ constexpr int LAMP = 20;
 #endif
 constexpr int KB = SHM_F32_KB;  // column nodes per laminate read in phase B (divides 6)
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// --- mbarrier and bulk copies (one CTA, no cluster) -------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+// waits for the phase with the given parity; gives up after a bounded number
+// of polls (returns false) instead of spinning for ever
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < (1 << 16); ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// One line of floats to copy: global element indices [lo, hi) of `base`
+// (lo >= 0), to be read back as column c of the line at smem[c + off] where
+// `origin` is the global index of column 0.  The copy is rounded out to
+// 16-byte boundaries (base is 16-byte aligned): it starts at lo & ~3 and
+// moves whole 16-byte units, so off = origin - (lo & ~3).
+struct Line {
+  const float* src;
+  unsigned bytes;
+  int off;
+};
+__device__ __forceinline__ Line line_of(const float* base, long long origin, long long lo, long long hi) {
+  Line l;
+  const long long a = lo & ~3LL, e = (hi + 3) & ~3LL;
+  l.src = base + a;
+  l.bytes = hi > lo ? (unsigned)((e - a) * 4) : 0u;
+  l.off = (int)(origin - a);
+  return l;
+}
+
 template <int EW> struct F32Geom {
   static constexpr int G = 32 / EW;
-  static constexpr int W = 5 * EW + 1;          // band columns
-  static constexpr int OWN = 5 * (EW - 1);      // owned columns
-  static constexpr int URING = 11;              // u_n node rows kept
-  static constexpr int URAW = URING * 5 * W;
-  static constexpr int UGS = URAW + ((16 - URAW % 32) + 64) % 32;   // group stride = 16 mod 32
+  static constexpr int W = 5 * EW + 1;               // band columns
+  static constexpr int OWN = 5 * (EW - 1);           // owned columns
+  static constexpr int WP = (W + 6 + 3) / 4 * 4;     // ring line stride (floats): W + alignment slack
+  static constexpr int OWNP = (OWN + 6 + 3) / 4 * 4; // update-operand line stride
+  static constexpr int URING = 11;                   // u_n node rows kept
+  static constexpr int URAW = URING * 5 * WP;
+  static constexpr int UGS = URAW + ((16 - URAW % 32) + 64) % 32;   // group stride = 16 mod 32 (a multiple of 4)
+  static constexpr int PVS = 5 * 5 * OWNP;           // u_{n-1} of the 5 node rows a row completes
+  static constexpr int MVS = 5 * 2 * OWNP;           // their inverse masses (translational, rotational)
   static constexpr int FRAW = 6 * 5 * W;
   static constexpr int FGS = FRAW + ((16 - FRAW % 32) + 64) % 32;
+  static constexpr int EDGE = 6 * 5 * CTA_ELEMS;     // column part of each lane's column 5 [row][field][lane]
+  static_assert(UGS % 4 == 0 && PVS % 4 == 0 && MVS % 4 == 0, "bulk-copy targets stay 16-byte aligned");
+};
+
+// shared-memory layout (floats): ys, vred, edge | ring | pv | mv | band | laminate pairs
+template <int EW> struct F32Smem {
+  using GM = F32Geom<EW>;
+  static constexpr int YS = 0;
+  static constexpr int VRED = CTA_ELEMS * ELEM_STRIDE;
+  static constexpr int EDGE = VRED + NP * CTA_ELEMS;
+  static constexpr int RING = (EDGE + GM::EDGE + 3) / 4 * 4;
+  static constexpr int PV = RING + GM::G * GM::UGS;
+  static constexpr int MV = PV + GM::G * GM::PVS;
+  static constexpr int BAND = MV + GM::G * GM::MVS;
+  static constexpr int LAM = (BAND + GM::G * GM::FGS + 1) / 2 * 2;
+  static constexpr int END = LAM + 2 * LAMP * CTA_ELEMS;
 };
 
 template <int EW>
 constexpr size_t struct_f32_smem_bytes() {
-  using GM = F32Geom<EW>;
-  return sizeof(float) * (2 * CTA_ELEMS * ELEM_STRIDE + NP * CTA_ELEMS + GM::G * (GM::UGS + GM::FGS)) +
-         sizeof(float2) * 2 * LAMP * CTA_ELEMS;
+  return sizeof(float) * F32Smem<EW>::END;
 }
 
 struct F32Args {
@@ -155,61 +225,61 @@ __device__ __forceinline__ const GroupTask& pick(const GroupTask* gt, int g) {
   }
 }
 
-// copy node rows [r0, r0+NR) (relative to the task's first node row) of u_n
-// into ring slots slot0, slot0+1, ... (mod URING); warp f < 5 copies field f
-// of every lane group; columns outside the plate are left untouched (never
-// read).  colmask bit (gg*8 + chunk) says whether this lane's column
-// chunk*32 + lane of group gg lies on the plate (fixed for a task).
+// Issues, from warp 0, the bulk copies of one phase of the CTA's mbarrier and
+// arrives on it with their byte count:
+//  * ring lines: u_n node rows [r0, r0 + nr) of the task (relative to its first
+//    node row 5 eyA), all five fields, into ring slots slot0, slot0 + 1, ...;
+//  * update lines (upd >= 0): u_{n-1} (five fields) and the two inverse-mass
+//    lines of node rows 5 (eyA + upd) + jj, jj = 0..4, of the band rows that
+//    element row `upd` completes (owned columns only).
+// Rows off the plate, and update rows the task does not own, are skipped.
 template <int EW>
-__device__ __forceinline__ unsigned ring_colmask(const GroupTask* gt) {
+__device__ __forceinline__ void issue_lines(const F32Args& a, const GroupTask* gt, const float* cur,
+                                            const float* prev, float* ring, float* pv, float* mv, int* roff,
+                                            int* poff, unsigned bar, int r0, int nr, int slot0, int upd) {
   using GM = F32Geom<EW>;
+  constexpr int G = GM::G, UR = GM::URING;
   const int lane = threadIdx.x & 31;
-  unsigned m = 0;
-#pragma unroll
-  for (int gg = 0; gg < GM::G; ++gg) {
-    const GroupTask& t = pick<GM::G>(gt, gg);
-    const int col0 = 5 * (t.strip * (EW - 1) - 1);
-#pragma unroll
-    for (int ch = 0; ch * 32 < GM::W; ++ch) {
-      const int c = ch * 32 + lane;
-      if (t.has && c < GM::W && (unsigned)(col0 + c) < (unsigned)t.NX) m |= 1u << (gg * 8 + ch);
-    }
-  }
-  return m;
-}
-
-template <int EW, int NR>
-__device__ __forceinline__ void ring_load(float* ring, const float* __restrict__ cur, int64_t nnode_pad,
-                                          const GroupTask* gt, int r0, int slot0, unsigned colmask) {
-  using GM = F32Geom<EW>;
-  constexpr int G = GM::G, W = GM::W, UR = GM::URING;
-  const int f = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (f >= 5) return;
-#pragma unroll
-  for (int gg = 0; gg < G; ++gg) {
-    const GroupTask& t = pick<G>(gt, gg);
-    if (!t.has) continue;
-    const int col0 = 5 * (t.strip * (EW - 1) - 1);
-    const int row0 = 5 * t.eyA + r0;
-    const int NX = t.NX, rmax = 5 * t.ney;
-    const float* src = cur + f * nnode_pad + t.node0 + (int64_t)row0 * NX + col0 + lane;
-    const unsigned dbase =
-        static_cast<unsigned>(__cvta_generic_to_shared(ring + gg * GM::UGS + f * W + lane));
-    int sl = slot0;
-#pragma unroll
-    for (int rr = 0; rr < NR; ++rr) {
-      if (row0 + rr <= rmax) {
-        const unsigned drow = dbase + (unsigned)(sl * 5 * W) * 4u;
-#pragma unroll
-        for (int ch = 0; ch * 32 < W; ++ch)
-          if (colmask & (1u << (gg * 8 + ch)))
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(drow + ch * 128u), "l"(src + ch * 32)
-                         : "memory");
+  const int nring = G * nr * 5;
+  const int ntot = nring + (upd >= 0 ? G * 5 * 7 : 0);
+  unsigned bytes = 0;
+  for (int k = lane; k < ntot; k += 32) {
+    Line l;
+    unsigned dst;
+    if (k < nring) {
+      const int gg = k / (nr * 5), rem = k % (nr * 5), rr = rem / 5, f = rem % 5;
+      const GroupTask& t = gt[gg];
+      const int row = 5 * t.eyA + r0 + rr;
+      int sl = slot0 + rr;
+      if (sl >= UR) sl -= UR;
+      const long long origin = t.node0 + (long long)row * t.NX + 5 * (t.strip * (EW - 1) - 1);
+      const long long rowbeg = t.node0 + (long long)row * t.NX;
+      const long long lo = max(origin, rowbeg), hi = min(origin + GM::W, rowbeg + t.NX);
+      l = line_of(cur + f * a.nnode_pad, origin, lo, (t.has && row <= 5 * t.ney) ? hi : lo);
+      dst = smem_u32(ring + gg * GM::UGS + (sl * 5 + f) * GM::WP);
+      if (f == 0) roff[gg * UR + sl] = l.off;
+    } else {
+      const int k2 = k - nring, gg = k2 / 35, rem = k2 % 35, jj = rem / 7, w = rem % 7;
+      const GroupTask& t = gt[gg];
+      const int row = 5 * (t.eyA + upd) + jj;
+      const bool own = t.has && upd < t.nrows && (t.block == 0 || upd > 0);
+      const int ix0 = 5 * t.strip * (EW - 1);
+      const long long origin = t.node0 + (long long)row * t.NX + ix0;
+      const long long hi = origin + min(GM::OWN, t.NX - ix0);
+      if (w < 5) {
+        l = line_of(prev + w * a.nnode_pad, origin, origin, own ? hi : origin);
+        dst = smem_u32(pv + gg * GM::PVS + (jj * 5 + w) * GM::OWNP);
+      } else {
+        l = line_of(a.minv + (w - 5) * a.nnode_pad, origin, origin, own ? hi : origin);
+        dst = smem_u32(mv + gg * GM::MVS + (jj * 2 + (w - 5)) * GM::OWNP);
       }
-      src += NX;
-      if (++sl == UR) sl = 0;
+      if (w == 0) poff[gg * 5 + jj] = l.off;
     }
+    bytes += l.bytes;
+    if (l.bytes) bulk_g2s(dst, l.src, l.bytes, bar);
   }
+  bytes = __reduce_add_sync(0xffffffffu, bytes);
+  if (lane == 0) mbar_arrive_tx(bar, bytes);
 }
 
 // kAdj: the adjoint step of the same operator (K symmetric): lambda in
@@ -219,19 +289,29 @@ __device__ __forceinline__ void ring_load(float* ring, const float* __restrict__
 template <int EW, bool kSensor, bool kAdj = false>
 __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, int kstep) {
   using GM = F32Geom<EW>;
+  using SM = F32Smem<EW>;
   constexpr int G = GM::G;
   constexpr int W = GM::W;
+  constexpr int WP = GM::WP;
   constexpr int OWN = GM::OWN;
   constexpr int NCOL = (OWN + 31) / 32;  // update passes over a band row's owned columns
   constexpr int UR = GM::URING;
   extern __shared__ __align__(16) unsigned char smraw[];
   float* sm = reinterpret_cast<float*>(smraw);
-  float* vred = sm + 2 * CTA_ELEMS * ELEM_STRIDE;
-  float* ring = vred + NP * CTA_ELEMS;
-  float* band = ring + G * GM::UGS;
-  // laminate pairs of a row's elements, two buffers [2][LAMP][lane] (row r in
-  // buffer r & 1, copied at the top of row r - 1)
-  float2* lsm = reinterpret_cast<float2*>(band + G * GM::FGS);
+  float* vred = sm + SM::VRED;
+  float* edge = sm + SM::EDGE;
+  float* ring = sm + SM::RING;
+  float* pv = sm + SM::PV;
+  float* mv = sm + SM::MV;
+  float* band = sm + SM::BAND;
+  // laminate pairs of the row's elements [LAMP][lane], copied after the
+  // previous row's last read of them
+  float2* lsm = reinterpret_cast<float2*>(sm + SM::LAM);
+  __shared__ __align__(8) unsigned long long bar_mem;
+  __shared__ int roff[G * UR];  // ring slot -> smem offset of relative column 0
+  __shared__ int poff[G * 5];   // update row -> smem offset of owned column 0
+  __shared__ GroupTask gt[G];   // task facts of the lane groups (shared, not in registers)
+  const unsigned bar = smem_u32(&bar_mem);
 
   const int nn = *a.d_base + kstep;
   const bool odd = ((nn - a.nn_first) & 1);
@@ -246,30 +326,26 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   const int lane = threadIdx.x & 31;
   const int g = lane / EW;
   const int q = lane % EW;
-  float* xs = sm + lane * ELEM_STRIDE;
-  float* ys = sm + (CTA_ELEMS + lane) * ELEM_STRIDE;
+  float* ys = sm + SM::YS + lane * ELEM_STRIDE;
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   const bool guard = guard_step(a.fs, nn);
   const int ntg = (a.ntask + G - 1) / G;
-  bool bad = false;
-  // update prefetch: warp j finalises logical band row j of every lane group,
-  // owned columns c = lane + 32*s
-  float uo_r[G][NCOL][5];
-  float mt_r[G][NCOL], mr_r[G][NCOL];
+  bool bad = false, late = false;
+  unsigned phase = 0;      // parity of the mbarrier phase to wait for next
   bool gpend = false;      // adjoint: an element's gradient partials await reduction
   long long gpend_e = 0;   // (its grid-order index)
+  if (threadIdx.x == 0) mbar_init(bar, 1);
 
   // copy the lane's element's laminate pairs (warp j: pairs j, j+6, ...)
-  auto lam_load = [&](int buf, int mat) {
+  auto lam_load = [&](int mat) {
     const float2* mp = a.matp + (int64_t)mat * LAMP;
-    float2* d = lsm + buf * LAMP * CTA_ELEMS + lane;
+    float2* d = lsm + lane;
     for (int c = j; c < LAMP; c += CTA_THREADS / 32) {
-      const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(d + c * CTA_ELEMS));
+      const unsigned s = smem_u32(d + c * CTA_ELEMS);
       asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(mp + c) : "memory");
     }
   };
 
-  __shared__ GroupTask gt[G];  // task facts of the lane groups (shared, not in registers)
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
     __syncthreads();
     if (threadIdx.x < G) gt[threadIdx.x] = load_group_task(a, tg * G + threadIdx.x);
@@ -285,6 +361,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     const long long eg0 = t.egrid0 + (long long)t.eyA * t_nex + ex;
     const float t_sx = t.sx, t_sy = t.sy, t_area4 = t.area4;
     float* ub = ring + g * GM::UGS;
+    const int* uoff = roff + g * UR;
     float* fb = band + g * GM::FGS;
     const float2 wsxy = make_float2(t_sx, t_sy);
     // band row j of group gg is final at element rows r in [ulo, uhi), and
@@ -312,27 +389,31 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     for (int gg = 0; gg < G; ++gg) fcur[gg] = pick<G>(gt, gg).f0;
 
     for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
-    const unsigned colmask = ring_colmask<EW>(gt);
-    ring_load<EW, 6>(ring, cur, a.nnode_pad, gt, 0, 0, colmask);
+    // the task's first six node rows (one mbarrier phase, waited at row 0)
+    if (j == 0 && maxrows > 0) issue_lines<EW>(a, gt, cur, prev, ring, pv, mv, roff, poff, bar, 0, 6, 0, -1);
     // row 0's laminate pairs; the material index two rows ahead and the
     // stiffness factor one row ahead are read into registers
     int mnext = 0;
     float keep = 1.f, knext = 1.f;
     if (t_nrows > 0 && colok) {
-      lam_load(0, a.emat_g[eg0]);
+      lam_load(a.emat_g[eg0]);
       keep = a.ekeep_g[eg0];
     }
     if (t_nrows > 1 && colok) mnext = a.emat_g[eg0 + t_nex];
     cp_async_commit();
+    if (maxrows > 0) {
+      if (!late) late = !mbar_wait(bar, phase);  // after one timeout, no further waits
+      phase ^= 1u;
+    }
 
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
     int rb6 = 0;  // r mod 6
     for (int r = 0; r < maxrows; ++r) {
-      // this row's node rows have landed (the only copy group in flight); the
-      // barrier also ends the previous row's update for every warp, so the
-      // ring slots of the previous row's first five node rows are free: the
-      // next element row's five new node rows (5r+6 .. 5r+10) go there
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      // the row's laminate pairs have landed (its node rows came with the
+      // previous phase); the barrier also ends the previous row's update for
+      // every warp, so the ring slots of the previous row's first five node
+      // rows and the update-operand lines are free
+      cp_async_wait_all();
       __syncthreads();
       if (kAdj && gpend) {  // previous element row's gradient partials are complete
         double sum = 0.0;
@@ -341,23 +422,21 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         a.grad[a.e_of_g[gpend_e]] -= sum;
         gpend = false;
       }
+      // one phase: the next element row's five new node rows (5r+6 .. 5r+10)
+      // and this row's update operands; waited for before the update
+      if (j == 0)
+        issue_lines<EW>(a, gt, cur, prev, ring, pv, mv, roff, poff, bar, 5 * r + 6, r + 1 < maxrows ? 5 : 0,
+                        rb + 6 >= UR ? rb + 6 - UR : rb + 6, r);
       const bool rowact = r < t_nrows;
       const bool valid = rowact && colok;
       const long long egrid = eg0 + (long long)r * t_nex;
-      // the next row's laminate pairs go to the other buffer (last read in the
-      // previous row's phase B)
-      if (r + 1 < maxrows) {
-        ring_load<EW, 5>(ring, cur, a.nnode_pad, gt, 5 * r + 6, rb + 6 >= UR ? rb + 6 - UR : rb + 6, colmask);
-        if (r + 1 < t_nrows && colok) lam_load((r + 1) & 1, mnext);
-      }
-      cp_async_commit();
       if (r + 1 < t_nrows && colok) knext = a.ekeep_g[egrid + t_nex];
-      if (r + 2 < t_nrows && colok) mnext = a.emat_g[egrid + 2 * t_nex];
       auto slot = [rb](int k) { const int s = rb + k; return s >= UR ? s - UR : s; };
 
       // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
       if (valid) {
-        const float* urow = ub + slot(j) * 5 * W + 5 * q;
+        const int sj = slot(j);
+        const float* urow = ub + sj * 5 * WP + uoff[sj] + 5 * q;
         float2 acc[5][3];
 #pragma unroll
         for (int f = 0; f < 5; ++f)
@@ -367,7 +446,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         for (int k = 0; k < NP; ++k)
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
-            const float2 u2 = bc2(urow[f * W + k]);
+            const float2 u2 = bc2(urow[f * WP + k]);
 #pragma unroll
             for (int p = 0; p < 3; ++p) acc[f][p] = fma2(c_Dp[k][p], u2, acc[f][p]);
           }
@@ -382,151 +461,180 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           }
       }
       __syncthreads();
-      // phase B: column i = j
-      if (valid) {
+      // band row of logical row m of this element row (row 0 carries the
+      // previous element row's top line)
+      auto prow_of = [rb6](int m) { const int p = m - rb6; return p < 0 ? p + 6 : p; };
+      float dl = 0.f;  // adjoint: this thread's share of the element's gradient partial
+      // phase B: column i = j; the column part of the transposed operator goes
+      // straight into the band (column 5 of a lane is column 0 of the next
+      // lane's element: kept in `edge` for it, except at the strip's end)
+      {
         const int i = j;
-        float v[5][NP];
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-          const float* urow = ub + slot(k) * 5 * W + 5 * q + i;
-#pragma unroll
-          for (int f = 0; f < 5; ++f) v[f][k] = urow[f * W];
-        }
-        // eta-derivatives, packed over node pairs, scaled by 2/ay
-        float2 de2[5][3];
-#pragma unroll
-        for (int f = 0; f < 5; ++f) {
-#pragma unroll
-          for (int p = 0; p < 3; ++p) de2[f][p] = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int m = 0; m < NP; ++m) {
-            const float2 v2 = bc2(v[f][m]);
-#pragma unroll
-            for (int p = 0; p < 3; ++p) de2[f][p] = fma2(c_Dp[m][p], v2, de2[f][p]);
-          }
-#pragma unroll
-          for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
-        }
-        const float2* L = lsm + (r & 1) * LAMP * CTA_ELEMS + lane;  // pair c at L[c * CTA_ELEMS]
-        // the stiffness factor scales the element's fluxes (K_e^0 for the adjoint)
-        const float akeep = kAdj ? t_area4 : t_area4 * keep;
         float2 Fe2[5][3];
 #pragma unroll
         for (int f = 0; f < 5; ++f)
 #pragma unroll
           for (int p = 0; p < 3; ++p) Fe2[f][p] = make_float2(0.f, 0.f);
         float vp = 0.f;
-        // nodes k of the column in blocks of KB: each laminate pair is read
-        // from shared memory once per block (the products keep their order)
+        if (valid) {
+          float v[5][NP];
 #pragma unroll
-        for (int k0 = 0; k0 < NP; k0 += KB) {
-          // strains: ex, ey, gxy, kx, ky, kxy, gyz, gxz
-          float sn[KB][8];
+          for (int k = 0; k < NP; ++k) {
+            const int sk = slot(k);
+            const float* urow = ub + sk * 5 * WP + uoff[sk] + 5 * q + i;
 #pragma unroll
-          for (int kk = 0; kk < KB; ++kk) {
-            const int k = k0 + kk;
-            float gx[5], gy[5];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-              gx[f] = ys[f * NPE + i * NP + k];
-              gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
-            }
-            sn[kk][0] = gx[0];
-            sn[kk][1] = gy[2];
-            sn[kk][2] = gy[0] + gx[2];
-            sn[kk][3] = gx[1];
-            sn[kk][4] = gy[3];
-            sn[kk][5] = gy[1] + gx[3];
-            sn[kk][6] = v[3][k] + gy[4];
-            sn[kk][7] = v[1][k] + gx[4];
-            if (kSensor) {
-              vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
-            }
+            for (int f = 0; f < 5; ++f) v[f][k] = urow[f * WP];
           }
-          // R[0] = (Nxx, Nyy), R[1] = (Nxy, Mxx), R[2] = (Myy, Mxy), R[3] = (Qy, Qx)
-          float2 R[4][KB];
+          // eta-derivatives, packed over node pairs, scaled by 2/ay
+          float2 de2[5][3];
 #pragma unroll
-          for (int b = 0; b < 3; ++b)
+          for (int f = 0; f < 5; ++f) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-              const float2 l = L[(6 * b + c) * CTA_ELEMS];
+            for (int p = 0; p < 3; ++p) de2[f][p] = make_float2(0.f, 0.f);
 #pragma unroll
-              for (int kk = 0; kk < KB; ++kk)
-                R[b][kk] = c == 0 ? mul2(l, bc2(sn[kk][c])) : fma2(l, bc2(sn[kk][c]), R[b][kk]);
+            for (int m = 0; m < NP; ++m) {
+              const float2 v2 = bc2(v[f][m]);
+#pragma unroll
+              for (int p = 0; p < 3; ++p) de2[f][p] = fma2(c_Dp[m][p], v2, de2[f][p]);
             }
-          {
-            const float2 l18 = L[18 * CTA_ELEMS], l19 = L[19 * CTA_ELEMS];
 #pragma unroll
-            for (int kk = 0; kk < KB; ++kk) R[3][kk] = fma2(l19, bc2(sn[kk][7]), mul2(l18, bc2(sn[kk][6])));
+            for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
           }
+          const float2* L = lsm + lane;  // pair c at L[c * CTA_ELEMS]
+          // the stiffness factor scales the element's fluxes (K_e^0 for the adjoint)
+          const float akeep = kAdj ? t_area4 : t_area4 * keep;
+          // nodes k of the column in blocks of KB: each laminate pair is read
+          // from shared memory once per block (the products keep their order)
 #pragma unroll
-          for (int kk = 0; kk < KB; ++kk) {
-            const int k = k0 + kk;
-            const float2 NN = R[0][kk], NM = R[1][kk], MM = R[2][kk], QQ = R[3][kk];
-            const float Wn = c_w32[i] * c_w32[k] * akeep;
-            const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
-            // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
-            const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
-            const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
-            const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
-            const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
-            const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
-            const float2 Gs[5] = {G0, G1, G2, G3, G4};
+          for (int k0 = 0; k0 < NP; k0 += KB) {
+            // strains: ex, ey, gxy, kx, ky, kxy, gyz, gxz
+            float sn[KB][8];
 #pragma unroll
-            for (int f = 0; f < 5; ++f) {
-              ys[f * NPE + i * NP + k] = Gs[f].x;
-              const float2 ge = bc2(Gs[f].y);
+            for (int kk = 0; kk < KB; ++kk) {
+              const int k = k0 + kk;
+              float gx[5], gy[5];
 #pragma unroll
-              for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
+              for (int f = 0; f < 5; ++f) {
+                gx[f] = ys[f * NPE + i * NP + k];
+                gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
+              }
+              sn[kk][0] = gx[0];
+              sn[kk][1] = gy[2];
+              sn[kk][2] = gy[0] + gx[2];
+              sn[kk][3] = gx[1];
+              sn[kk][4] = gy[3];
+              sn[kk][5] = gy[1] + gx[3];
+              sn[kk][6] = v[3][k] + gy[4];
+              sn[kk][7] = v[1][k] + gx[4];
+              if (kSensor) {
+                vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
+              }
             }
-            if (k & 1) {
-              Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
-              Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
-            } else {
-              Fe2[1][k >> 1].x += Wn * QQ.y;
-              Fe2[3][k >> 1].x += Wn * QQ.x;
+            // R[0] = (Nxx, Nyy), R[1] = (Nxy, Mxx), R[2] = (Myy, Mxy), R[3] = (Qy, Qx)
+            float2 R[4][KB];
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+#pragma unroll
+              for (int c = 0; c < 6; ++c) {
+                const float2 l = L[(6 * b + c) * CTA_ELEMS];
+#pragma unroll
+                for (int kk = 0; kk < KB; ++kk)
+                  R[b][kk] = c == 0 ? mul2(l, bc2(sn[kk][c])) : fma2(l, bc2(sn[kk][c]), R[b][kk]);
+              }
+            {
+              const float2 l18 = L[18 * CTA_ELEMS], l19 = L[19 * CTA_ELEMS];
+#pragma unroll
+              for (int kk = 0; kk < KB; ++kk) R[3][kk] = fma2(l19, bc2(sn[kk][7]), mul2(l18, bc2(sn[kk][6])));
+            }
+#pragma unroll
+            for (int kk = 0; kk < KB; ++kk) {
+              const int k = k0 + kk;
+              const float2 NN = R[0][kk], NM = R[1][kk], MM = R[2][kk], QQ = R[3][kk];
+              const float Wn = c_w32[i] * c_w32[k] * akeep;
+              const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
+              // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
+              const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
+              const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
+              const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
+              const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
+              const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
+              const float2 Gs[5] = {G0, G1, G2, G3, G4};
+#pragma unroll
+              for (int f = 0; f < 5; ++f) {
+                ys[f * NPE + i * NP + k] = Gs[f].x;
+                const float2 ge = bc2(Gs[f].y);
+#pragma unroll
+                for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
+              }
+              if (k & 1) {
+                Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
+                Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
+              } else {
+                Fe2[1][k >> 1].x += Wn * QQ.y;
+                Fe2[3][k >> 1].x += Wn * QQ.x;
+              }
             }
           }
         }
+        if (kSensor && valid) vred[i * CTA_ELEMS + lane] = vp;
+        if constexpr (kAdj) {
+          // column i's share of lambda' K_e^0 u_{n-1} (the row part is added
+          // in phase C), then keep_e K_e^0 lambda
+          if (valid) {
+            const float* umc = a.um + t.node0 + (int64_t)(5 * (t.eyA + r)) * t.NX + 5 * ex + i;
 #pragma unroll
-        for (int f = 0; f < 5; ++f)
+            for (int f = 0; f < 5; ++f)
 #pragma unroll
-          for (int p = 0; p < 3; ++p) {
-            xs[f * NPE + i * NP + 2 * p] = Fe2[f][p].x;
-            xs[f * NPE + i * NP + 2 * p + 1] = Fe2[f][p].y;
+              for (int p = 0; p < 3; ++p) {
+                dl += Fe2[f][p].x * umc[f * a.nnode_pad + (2 * p) * t.NX];
+                dl += Fe2[f][p].y * umc[f * a.nnode_pad + (2 * p + 1) * t.NX];
+              }
+#pragma unroll
+            for (int f = 0; f < 5; ++f)
+#pragma unroll
+              for (int p = 0; p < 3; ++p) Fe2[f][p] = mul2(Fe2[f][p], bc2(keep));
           }
-        if (kSensor) vred[i * CTA_ELEMS + lane] = vp;
+        }
+        // column part at rows m = 0..5 of column i (zeros from lanes without
+        // an element, so that stale band values never survive)
+        if (i < 5 || q == EW - 1) {
+          float* col = fb + 5 * q + i;
+          int pr[6];
+#pragma unroll
+          for (int m = 0; m < 6; ++m) pr[m] = prow_of(m) * 5 * W;
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            col[pr[0] + f * W] += Fe2[f][0].x;   // the carried row: added to
+            col[pr[1] + f * W] = Fe2[f][0].y;
+            col[pr[2] + f * W] = Fe2[f][1].x;
+            col[pr[3] + f * W] = Fe2[f][1].y;
+            col[pr[4] + f * W] = Fe2[f][2].x;
+            col[pr[5] + f * W] = Fe2[f][2].y;
+          }
+        } else {
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              edge[((2 * p) * 5 + f) * CTA_ELEMS + lane] = Fe2[f][p].x;
+              edge[((2 * p + 1) * 5 + f) * CTA_ELEMS + lane] = Fe2[f][p].y;
+            }
+        }
       }
       __syncthreads();
+      // the next row's laminate pairs replace this row's (read above)
+      if (r + 1 < t_nrows && colok) lam_load(mnext);
+      cp_async_commit();
+      if (r + 2 < t_nrows && colok) mnext = a.emat_g[egrid + 2 * t_nex];
 
-      // the update's global loads for band row j, issued before phase C
-      bool rowok[G];
-      long long rowbase[G];
-#pragma unroll
-      for (int gg = 0; gg < G; ++gg) {
-        rowok[gg] = r >= ulo[gg] && r < uhi[gg];
-        rowbase[gg] = ub0[gg] + (long long)r * ustr[gg];
-#pragma unroll
-        for (int s = 0; s < NCOL; ++s) {
-          const int c = lane + 32 * s;
-          if (rowok[gg] && c < ucol[gg]) {
-            const long long node = rowbase[gg] + c;
-            mt_r[gg][s] = a.minv[node];
-            mr_r[gg][s] = a.minv[a.nnode_pad + node];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) uo_r[gg][s][f] = prev[f * a.nnode_pad + node];
-          }
-        }
-      }
-
-      // phase C: xi-part of the transposed operator + column part
+      // phase C: xi-part of the transposed operator, added to the band
       float out[5][NP];
       if (valid) {
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
           float2 o2[3];
 #pragma unroll
-          for (int p = 0; p < 3; ++p) o2[p] = make_float2(xs[f * NPE + (2 * p) * NP + j], xs[f * NPE + (2 * p + 1) * NP + j]);
+          for (int p = 0; p < 3; ++p) o2[p] = make_float2(0.f, 0.f);
 #pragma unroll
           for (int ii = 0; ii < NP; ++ii) {
             const float2 gg2 = bc2(ys[f * NPE + ii * NP + j]);
@@ -540,9 +648,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           }
         }
         if constexpr (kAdj) {
-          // line j's share of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
+          // line j's row part of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
           const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
-          float dl = 0.f;
 #pragma unroll
           for (int f = 0; f < 5; ++f)
 #pragma unroll
@@ -558,45 +665,32 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
 #pragma unroll
           for (int i = 0; i < NP; ++i) out[f][i] = 0.f;
       }
-      // band accumulation.  Logical row j of this element row is physical row
-      // (j - r) mod 6.  Row 0 carries the previous element row's top line and
-      // is added to; rows 1..5 start here and are stored.  Column i = 5 of a
-      // lane's element is column 0 of the next lane's: it moves one lane up
-      // by shuffle (lanes of a group are consecutive), and the strip's last
-      // lane writes it itself.
-      int prow = j - rb6;
-      if (prow < 0) prow += 6;
+      // band accumulation: logical row j of this element row is physical row
+      // (j - r) mod 6 and already holds the column part (phase B).  Column
+      // i = 5 of a lane's element is column 0 of the next lane's: its row
+      // part moves one lane up by shuffle and its column part comes from
+      // `edge`; the strip's last lane adds it itself.
+      const int prow = prow_of(j);
       {
-        float* dst = fb + prow * 5 * W + 5 * q;
+        float* bdst = fb + prow * 5 * W + 5 * q;
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
           const float from_left = __shfl_up_sync(0xffffffffu, out[f][5], 1);
-          if (q > 0) out[f][0] += from_left;
+          if (q > 0) out[f][0] += from_left + edge[(j * 5 + f) * CTA_ELEMS + lane - 1];
         }
-        if (j == 0) {
 #pragma unroll
-          for (int f = 0; f < 5; ++f)
+        for (int f = 0; f < 5; ++f)
 #pragma unroll
-            for (int i = 0; i < 5; ++i) dst[f * W + i] += out[f][i];
-          if (q == EW - 1) {
+          for (int i = 0; i < 5; ++i) bdst[f * W + i] += out[f][i];
+        if (q == EW - 1) {
 #pragma unroll
-            for (int f = 0; f < 5; ++f) dst[f * W + 5] += out[f][5];
-          }
-        } else {
-#pragma unroll
-          for (int f = 0; f < 5; ++f)
-#pragma unroll
-            for (int i = 0; i < 5; ++i) dst[f * W + i] = out[f][i];
-          if (q == EW - 1) {
-#pragma unroll
-            for (int f = 0; f < 5; ++f) dst[f * W + 5] = out[f][5];
-          }
+          for (int f = 0; f < 5; ++f) bdst[f * W + 5] += out[f][5];
         }
-        // band row j is now complete and written by this warp alone (row 0
-        // adds the previous element row's line 5, stored before this row's
-        // first barrier), and warp j updates exactly band row j: a warp
-        // barrier suffices.  (The adjoint's gradient partials are reduced
-        // after the next CTA barrier.)
+        // band row j is now complete and written by this warp alone (the
+        // column parts of all warps were stored before the third barrier),
+        // and warp j updates exactly band row j: a warp barrier suffices.
+        // (The adjoint's gradient partials are reduced after the next CTA
+        // barrier.)
         __syncwarp();
       }
       if constexpr (!kAdj) {
@@ -638,21 +732,31 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           a.vsum[(int64_t)sl * a.nft + (nn - 1)] = sum;
         }
       }
-      // update owned, complete nodes of band row j (excitation added here by
-      // the node's owner)
+      // this row's update operands (and the next row's node rows) have landed
+      if (!late) late = !mbar_wait(bar, phase);
+      phase ^= 1u;
+      // update owned, complete nodes of band row j (excitation subtracted
+      // above by the node's owner)
 #pragma unroll
-      for (int gg = 0; gg < G; ++gg)
+      for (int gg = 0; gg < G; ++gg) {
+        if (!(r >= ulo[gg] && r < uhi[gg])) continue;
+        const long long rowbase = ub0[gg] + (long long)r * ustr[gg];
+        const float* urow = ring + gg * GM::UGS + slot(j) * 5 * WP + roff[gg * UR + slot(j)] + 5;
+        const float* bnd = band + gg * GM::FGS + prow * 5 * W + 5;
+        // u_{n-1} and 1/M from the phase's lines (node rows 0..4 of the band);
+        // the plate's top node row (j == 5) reads them from global memory
+        const int po = j < 5 ? poff[gg * 5 + j] : 0;
+        const float* pvr = pv + gg * GM::PVS + (j < 5 ? j : 0) * 5 * GM::OWNP + po;
+        const float* mvr = mv + gg * GM::MVS + (j < 5 ? j : 0) * 2 * GM::OWNP + po;
+        const GroupTask& t2 = pick<G>(gt, gg);
 #pragma unroll
         for (int s = 0; s < NCOL; ++s) {
           const int c = lane + 32 * s;
-          if (!(rowok[gg] && c < ucol[gg])) continue;
-          const float* bnd = band + gg * GM::FGS + prow * 5 * W + 5 + c;
-          const float* urow = ring + gg * GM::UGS + slot(j) * 5 * W + 5 + c;
-          const long long node = rowbase[gg] + c;
+          if (c >= ucol[gg]) continue;
+          const long long node = rowbase + c;
           float F[5];
 #pragma unroll
-          for (int f = 0; f < 5; ++f) F[f] = bnd[f * W];
-          const GroupTask& t2 = pick<G>(gt, gg);
+          for (int f = 0; f < 5; ++f) F[f] = bnd[f * W + c];
           if (kAdj && t2.on > 0) {
             const int iy = 5 * (t2.eyA + r) + j;
             for (int oi = t2.o0; oi < t2.o0 + t2.on; ++oi)
@@ -664,17 +768,26 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
               }
           }
           if (!kAdj && a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, node);
+          float mt, mr;
+          if (j < 5) {
+            mt = mvr[c];
+            mr = mvr[GM::OWNP + c];
+          } else {
+            mt = a.minv[node];
+            mr = a.minv[a.nnode_pad + node];
+          }
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
-            const float u = urow[f * W];
-            const float uo = uo_r[gg][s][f];
-            const float im = (f == 1 || f == 3) ? mr_r[gg][s] : mt_r[gg][s];
+            const float u = urow[f * WP + c];
+            const float uo = j < 5 ? pvr[f * GM::OWNP + c] : prev[f * a.nnode_pad + node];
+            const float im = (f == 1 || f == 3) ? mr : mt;
             const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
             dst[f * a.nnode_pad + node] = un;
             if (frame) store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
             if (guard && (!isfinite(un) || (f == 4 && u > a.blowup))) bad = true;
           }
         }
+      }
       // (the next row's first barrier separates this update from the ring
       // refill and the next band accumulation)
       keep = knext;
@@ -693,6 +806,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
     }
   }
   if (bad) atomicOr(a.flag, 1);
+  if (late) atomicOr(a.flag, 2);  // a bounded wait gave up: reported as SHM_ERR_TIMEOUT
 }
 
 }  // namespace shm

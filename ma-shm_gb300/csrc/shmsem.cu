@@ -1280,7 +1280,7 @@ extern "C" shm_status shm_plan_create(int32_t nscen, const shm_mesh* meshes, con
   p->fen = p->elem_off[nscen];
   if (p->nnode > INT32_MAX / 2 || p->fen * NPE > INT32_MAX / 2) return bad(p, "mesh too large for 32-bit slots");
   p->fen_pad = (p->fen + CTA_ELEMS - 1) / CTA_ELEMS * CTA_ELEMS;
-  p->nnode_pad = (p->nnode + 31) / 32 * 32;
+  p->nnode_pad = (p->nnode + 4 + 31) / 32 * 32;  // >= 4 spare floats: 16-byte-rounded line copies stay in the field
 
   // GLL constants
   std::vector<double> gx, gw, D;
@@ -1676,6 +1676,10 @@ static shm_status check_flag(shm_plan* p, cudaStream_t s) {
   int flag = 0;
   CKP(p, cudaMemcpyAsync(&flag, p->flag, 4, cudaMemcpyDeviceToHost, s));
   CKP(p, cudaStreamSynchronize(s));
+  if (flag & 2) {
+    p->err = "a bounded device-side wait gave up (bulk copies did not complete)";
+    return SHM_ERR_TIMEOUT;
+  }
   if (flag) {
     p->err = "integration error: blow-up or non-finite state detected";
     return SHM_ERR_DIVERGED;
@@ -1916,7 +1920,29 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
   steps = std::max(2, std::min(steps, avail - warm));
   if (steps < 2) return bad(p, "autotune: run too short");
   const int tiles[2] = {16, 32};
-  const int rows[5] = {4, 8, 16, 32, 64};
+  // rows per task: fixed candidates, and per tile the fewest rows with which
+  // every task of the plan is resident at once (one wave of two CTAs per SM)
+  // or in two waves -- a single large plate needs them to fill the GPU
+  std::vector<int> cand[2];
+  {
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || nsm < 1) nsm = 1;
+    for (int ti = 0; ti < 2; ++ti) {
+      cand[ti] = {4, 8, 16, 32, 64};
+      const int EW = tiles[ti], own = 5 * (EW - 1), G = 32 / EW;
+      auto ntask = [&](int H) {
+        long long n = 0;
+        for (const PlateDesc& pl : p->sp.h_plates) n += (long long)((pl.NX + own - 1) / own) * ((pl.ney + H - 1) / H);
+        return n;
+      };
+      for (int waves = 1; waves <= 2; ++waves)
+        for (int H = 1; H <= 64; ++H)
+          if (ntask(H) <= (long long)waves * 2 * nsm * G) {
+            if (std::find(cand[ti].begin(), cand[ti].end(), H) == cand[ti].end()) cand[ti].push_back(H);
+            break;
+          }
+    }
+  }
   float best = 1e30f;
   int bt = p->sp.tile, bh = p->sp.H;
   // candidate 0: the general element + node kernels
@@ -1933,8 +1959,8 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
     p->path = 2;
   }
   for (int ti = 0; ti < 2; ++ti)
-    for (int hi = 0; hi < 5; ++hi) {
-      shm_status st = struct_tasks(p, tiles[ti], rows[hi]);
+    for (int H : cand[ti]) {
+      shm_status st = struct_tasks(p, tiles[ti], H);
       if (st != SHM_OK) return st;
       drop_graph(p);
       if ((st = shm_reset(p)) != SHM_OK) return st;
@@ -1944,7 +1970,7 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
       if (ms < best) {
         best = ms;
         bt = tiles[ti];
-        bh = rows[hi];
+        bh = H;
       }
     }
   shm_status st = SHM_OK;

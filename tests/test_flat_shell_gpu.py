@@ -140,7 +140,7 @@ def test_batch_equals_solo(pkg, path):
     for s in range(3):
         sc = pkg.workloads.random_plate(np.random.default_rng([1, s]), edge=6.25e-3, nmin=3, nmax=7)
         scs.append(sc)
-    dt = 1.0e-7
+    dt = 7.0e-8      # below the stability limit of 6.25 mm elements (7.2e-8)
     nft = 250
     for sc in scs:
         _, sc.signal = pkg.hanning_signal(dt, nft, sc.carrier / 5, sc.carrier)
@@ -221,7 +221,7 @@ def test_autotune_picks_a_config_and_keeps_results(pkg):
     run = pkg.RunConfig(dt=dt, nft=nft, eta_xy=4e2, eta_z=4e3, h=3.9e-3)
     plan = pkg.Plan(scs, run, precision=32, path=2, steps_per_graph=20)
     best = plan.autotune(5)
-    assert best["tile"] in (0, 16, 32) and best["rows_per_block"] in (4, 8, 16, 32, 64)
+    assert best["tile"] in (0, 16, 32) and 1 <= best["rows_per_block"] <= 64
     if best["tile"] == 0:
         assert plan.info["path"] == 1
     else:
