@@ -7,17 +7,20 @@
 //    node rows of the next element row arrive by TMA bulk copies
 //    (cp.async.bulk, one per node row and field, completed on an mbarrier)
 //    while the current row is computed, so the gather never waits on memory;
-//  * the update's operands of the row (u_{n-1} and the inverse mass of the
-//    node rows it completes) are bulk-copied into shared memory at the row's
-//    start, so their DRAM latency hides behind the row's element work;
+//  * the update's global loads (u_{n-1}, inverse mass) are issued before the
+//    transposed operator so that their latency overlaps it;
 //  * the 6x6 contractions, resultants and fluxes run on packed FP32x2 FMA
 //    (__ffma2_rn, two lanes of a 64-bit register pair per instruction);
 //  * the force band is a 6-row ring (the shared node row is carried by
 //    re-labelling, not copied); the column part of the transposed operator is
 //    written into it directly (phase B), the row part added on top (phase C);
-//  * the laminate pairs of the next row are copied with cp.async after the
-//    last read of the current row's; the material index is read two rows
-//    ahead and the stiffness factor one row ahead into registers.
+//  * the laminate pairs are read through the read-only data cache (the table
+//    holds a few materials, so all lanes of a warp usually read the same
+//    pair); material index and stiffness factor come one row ahead;
+//  * lanes without an element (the strip's left halo at the plate edge,
+//    lanes past the plate, rows past the task) run the same code on finite
+//    data with a zero stiffness factor, so the phases have no divergent
+//    branches and such lanes contribute exact zeros.
 // Every bulk copy starts and ends on a 16-byte boundary: it covers the needed
 // columns rounded out to 4 floats, and a per-row offset locates column 0.
 // Results equal the generic kernel's up to FP32 rounding order.
@@ -48,10 +51,8 @@ constexpr int LAMP = 20;
 #define SHM_F32_KB 3
 #endif
 constexpr int KB = SHM_F32_KB;  // column nodes per laminate read in phase B (divides 6)
+static_assert(NP % KB == 0, "laminate blocks cover the column");
 
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // --- mbarrier and bulk copies (one CTA, no cluster) -------------------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -108,30 +109,24 @@ template <int EW> struct F32Geom {
   static constexpr int W = 5 * EW + 1;               // band columns
   static constexpr int OWN = 5 * (EW - 1);           // owned columns
   static constexpr int WP = (W + 6 + 3) / 4 * 4;     // ring line stride (floats): W + alignment slack
-  static constexpr int OWNP = (OWN + 6 + 3) / 4 * 4; // update-operand line stride
   static constexpr int URING = 11;                   // u_n node rows kept
   static constexpr int URAW = URING * 5 * WP;
   static constexpr int UGS = URAW + ((16 - URAW % 32) + 64) % 32;   // group stride = 16 mod 32 (a multiple of 4)
-  static constexpr int PVS = 5 * 5 * OWNP;           // u_{n-1} of the 5 node rows a row completes
-  static constexpr int MVS = 5 * 2 * OWNP;           // their inverse masses (translational, rotational)
   static constexpr int FRAW = 6 * 5 * W;
   static constexpr int FGS = FRAW + ((16 - FRAW % 32) + 64) % 32;
   static constexpr int EDGE = 6 * 5 * CTA_ELEMS;     // column part of each lane's column 5 [row][field][lane]
-  static_assert(UGS % 4 == 0 && PVS % 4 == 0 && MVS % 4 == 0, "bulk-copy targets stay 16-byte aligned");
+  static_assert(UGS % 4 == 0 && WP % 4 == 0, "bulk-copy targets stay 16-byte aligned");
 };
 
-// shared-memory layout (floats): ys, vred, edge | ring | pv | mv | band | laminate pairs
+// shared-memory layout (floats): ys, vred, edge | ring | band
 template <int EW> struct F32Smem {
   using GM = F32Geom<EW>;
   static constexpr int YS = 0;
   static constexpr int VRED = CTA_ELEMS * ELEM_STRIDE;
   static constexpr int EDGE = VRED + NP * CTA_ELEMS;
   static constexpr int RING = (EDGE + GM::EDGE + 3) / 4 * 4;
-  static constexpr int PV = RING + GM::G * GM::UGS;
-  static constexpr int MV = PV + GM::G * GM::PVS;
-  static constexpr int BAND = MV + GM::G * GM::MVS;
-  static constexpr int LAM = (BAND + GM::G * GM::FGS + 1) / 2 * 2;
-  static constexpr int END = LAM + 2 * LAMP * CTA_ELEMS;
+  static constexpr int BAND = RING + GM::G * GM::UGS;
+  static constexpr int END = BAND + GM::G * GM::FGS;
 };
 
 template <int EW>
@@ -156,6 +151,7 @@ struct F32Args {
   const int* __restrict__ esens_g;
   const int* __restrict__ f_xl;
   const int* __restrict__ f_iy;
+  const int* __restrict__ f_rowptr;  // per task with forces: first entry of each node row (5 nrows + 2)
   const int* __restrict__ f_field;
   const double* __restrict__ f_val;
   const double* __restrict__ st;
@@ -184,7 +180,7 @@ struct F32Args {
 
 // per-group task facts, uniform inside the group
 struct GroupTask {
-  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, scen, o0, on;
+  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, fr0, scen, o0, on;
   long long node0, egrid0;
   float sx, sy, area4;
 };
@@ -205,6 +201,7 @@ __device__ __forceinline__ GroupTask load_group_task(const F32Args& a, int tid) 
   t.NX = pl.NX;
   t.f0 = tk.f0;
   t.fn = tk.fn;
+  t.fr0 = tk.fr0;
   t.o0 = tk.o0;
   t.on = tk.on;
   t.scen = pl.scen;
@@ -225,58 +222,32 @@ __device__ __forceinline__ const GroupTask& pick(const GroupTask* gt, int g) {
   }
 }
 
-// Issues, from warp 0, the bulk copies of one phase of the CTA's mbarrier and
-// arrives on it with their byte count:
-//  * ring lines: u_n node rows [r0, r0 + nr) of the task (relative to its first
-//    node row 5 eyA), all five fields, into ring slots slot0, slot0 + 1, ...;
-//  * update lines (upd >= 0): u_{n-1} (five fields) and the two inverse-mass
-//    lines of node rows 5 (eyA + upd) + jj, jj = 0..4, of the band rows that
-//    element row `upd` completes (owned columns only).
-// Rows off the plate, and update rows the task does not own, are skipped.
+// Issues, from one warp, the bulk copies of one phase of the CTA's mbarrier
+// and arrives on it with their byte count: u_n node rows [r0, r0 + nr) of
+// each lane group's task (relative to its first node row 5 eyA), all five
+// fields, into ring slots slot0, slot0 + 1, ...  Rows off the plate are
+// skipped; the slot's column offset goes to roff.
 template <int EW>
-__device__ __forceinline__ void issue_lines(const F32Args& a, const GroupTask* gt, const float* cur,
-                                            const float* prev, float* ring, float* pv, float* mv, int* roff,
-                                            int* poff, unsigned bar, int r0, int nr, int slot0, int upd) {
+__device__ __forceinline__ void issue_lines(const F32Args& a, const GroupTask* gt, const float* cur, float* ring,
+                                            int* roff, unsigned bar, int r0, int nr, int slot0) {
   using GM = F32Geom<EW>;
   constexpr int G = GM::G, UR = GM::URING;
   const int lane = threadIdx.x & 31;
-  const int nring = G * nr * 5;
-  const int ntot = nring + (upd >= 0 ? G * 5 * 7 : 0);
+  const int ntot = G * nr * 5;
   unsigned bytes = 0;
   for (int k = lane; k < ntot; k += 32) {
-    Line l;
-    unsigned dst;
-    if (k < nring) {
-      const int gg = k / (nr * 5), rem = k % (nr * 5), rr = rem / 5, f = rem % 5;
-      const GroupTask& t = gt[gg];
-      const int row = 5 * t.eyA + r0 + rr;
-      int sl = slot0 + rr;
-      if (sl >= UR) sl -= UR;
-      const long long origin = t.node0 + (long long)row * t.NX + 5 * (t.strip * (EW - 1) - 1);
-      const long long rowbeg = t.node0 + (long long)row * t.NX;
-      const long long lo = max(origin, rowbeg), hi = min(origin + GM::W, rowbeg + t.NX);
-      l = line_of(cur + f * a.nnode_pad, origin, lo, (t.has && row <= 5 * t.ney) ? hi : lo);
-      dst = smem_u32(ring + gg * GM::UGS + (sl * 5 + f) * GM::WP);
-      if (f == 0) roff[gg * UR + sl] = l.off;
-    } else {
-      const int k2 = k - nring, gg = k2 / 35, rem = k2 % 35, jj = rem / 7, w = rem % 7;
-      const GroupTask& t = gt[gg];
-      const int row = 5 * (t.eyA + upd) + jj;
-      const bool own = t.has && upd < t.nrows && (t.block == 0 || upd > 0);
-      const int ix0 = 5 * t.strip * (EW - 1);
-      const long long origin = t.node0 + (long long)row * t.NX + ix0;
-      const long long hi = origin + min(GM::OWN, t.NX - ix0);
-      if (w < 5) {
-        l = line_of(prev + w * a.nnode_pad, origin, origin, own ? hi : origin);
-        dst = smem_u32(pv + gg * GM::PVS + (jj * 5 + w) * GM::OWNP);
-      } else {
-        l = line_of(a.minv + (w - 5) * a.nnode_pad, origin, origin, own ? hi : origin);
-        dst = smem_u32(mv + gg * GM::MVS + (jj * 2 + (w - 5)) * GM::OWNP);
-      }
-      if (w == 0) poff[gg * 5 + jj] = l.off;
-    }
+    const int gg = k / (nr * 5), rem = k % (nr * 5), rr = rem / 5, f = rem % 5;
+    const GroupTask& t = gt[gg];
+    const int row = 5 * t.eyA + r0 + rr;
+    int sl = slot0 + rr;
+    if (sl >= UR) sl -= UR;
+    const long long rowbeg = t.node0 + (long long)row * t.NX;
+    const long long origin = rowbeg + 5 * (t.strip * (EW - 1) - 1);
+    const long long lo = max(origin, rowbeg), hi = min(origin + GM::W, rowbeg + t.NX);
+    const Line l = line_of(cur + f * a.nnode_pad, origin, lo, (t.has && row <= 5 * t.ney) ? hi : lo);
+    if (f == 0) roff[gg * UR + sl] = l.off;
     bytes += l.bytes;
-    if (l.bytes) bulk_g2s(dst, l.src, l.bytes, bar);
+    if (l.bytes) bulk_g2s(smem_u32(ring + gg * GM::UGS + (sl * 5 + f) * GM::WP), l.src, l.bytes, bar);
   }
   bytes = __reduce_add_sync(0xffffffffu, bytes);
   if (lane == 0) mbar_arrive_tx(bar, bytes);
@@ -301,15 +272,9 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float* vred = sm + SM::VRED;
   float* edge = sm + SM::EDGE;
   float* ring = sm + SM::RING;
-  float* pv = sm + SM::PV;
-  float* mv = sm + SM::MV;
   float* band = sm + SM::BAND;
-  // laminate pairs of the row's elements [LAMP][lane], copied after the
-  // previous row's last read of them
-  float2* lsm = reinterpret_cast<float2*>(sm + SM::LAM);
   __shared__ __align__(8) unsigned long long bar_mem;
   __shared__ int roff[G * UR];  // ring slot -> smem offset of relative column 0
-  __shared__ int poff[G * 5];   // update row -> smem offset of owned column 0
   __shared__ GroupTask gt[G];   // task facts of the lane groups (shared, not in registers)
   const unsigned bar = smem_u32(&bar_mem);
 
@@ -336,31 +301,29 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   long long gpend_e = 0;   // (its grid-order index)
   if (threadIdx.x == 0) mbar_init(bar, 1);
 
-  // copy the lane's element's laminate pairs (warp j: pairs j, j+6, ...)
-  auto lam_load = [&](int mat) {
-    const float2* mp = a.matp + (int64_t)mat * LAMP;
-    float2* d = lsm + lane;
-    for (int c = j; c < LAMP; c += CTA_THREADS / 32) {
-      const unsigned s = smem_u32(d + c * CTA_ELEMS);
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(mp + c) : "memory");
-    }
-  };
-
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
     __syncthreads();
     if (threadIdx.x < G) gt[threadIdx.x] = load_group_task(a, tg * G + threadIdx.x);
+    // columns that no copy of this task writes stay finite (lanes without an
+    // element read them)
+    for (int i = threadIdx.x; i < G * GM::UGS; i += blockDim.x) ring[i] = 0.f;
+    for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
     __syncthreads();
     int maxrows = 0;
 #pragma unroll
     for (int gg = 0; gg < G; ++gg) maxrows = max(maxrows, gt[gg].nrows);
-    // this lane's element column, kept in registers for the whole task
+    // the task's first six node rows (one mbarrier phase, waited at row 0)
+    if (j == 0 && maxrows > 0) issue_lines<EW>(a, gt, cur, ring, roff, bar, 0, 6, 0);
+    // this lane's element column, kept in registers for the whole task; a lane
+    // without an element reads the columns of the nearest lane that has one
     const GroupTask& t = pick<G>(gt, g);
     const int t_nrows = t.nrows, t_nex = t.nex;
     const int ex = t.strip * (EW - 1) - 1 + q;
     const bool colok = ex >= 0 && ex < t_nex;
+    const int qc = min(max(q, t.strip == 0 ? 1 : 0), t_nex - (t.strip * (EW - 1) - 1) - 1);
     const long long eg0 = t.egrid0 + (long long)t.eyA * t_nex + ex;
     const float t_sx = t.sx, t_sy = t.sy, t_area4 = t.area4;
-    float* ub = ring + g * GM::UGS;
+    float* ub = ring + g * GM::UGS + 5 * qc;
     const int* uoff = roff + g * UR;
     float* fb = band + g * GM::FGS;
     const float2 wsxy = make_float2(t_sx, t_sy);
@@ -384,36 +347,24 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       ucol[gg] = min(OWN, t2.NX - ix0);
     }
-    int fcur[G];  // next force entry of each lane group's task (warp j's node rows)
-#pragma unroll
-    for (int gg = 0; gg < G; ++gg) fcur[gg] = pick<G>(gt, gg).f0;
-
-    for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
-    // the task's first six node rows (one mbarrier phase, waited at row 0)
-    if (j == 0 && maxrows > 0) issue_lines<EW>(a, gt, cur, prev, ring, pv, mv, roff, poff, bar, 0, 6, 0, -1);
-    // row 0's laminate pairs; the material index two rows ahead and the
-    // stiffness factor one row ahead are read into registers
-    int mnext = 0;
-    float keep = 1.f, knext = 1.f;
+    // material and stiffness factor of the lane's element in the current
+    // row (factor 0 where there is no element), the next row's read ahead
+    int mcur = 0, mnext = 0;
+    float keep = 0.f, knext = 0.f;
     if (t_nrows > 0 && colok) {
-      lam_load(a.emat_g[eg0]);
+      mcur = a.emat_g[eg0];
       keep = a.ekeep_g[eg0];
-    }
-    if (t_nrows > 1 && colok) mnext = a.emat_g[eg0 + t_nex];
-    cp_async_commit();
-    if (maxrows > 0) {
-      if (!late) late = !mbar_wait(bar, phase);  // after one timeout, no further waits
-      phase ^= 1u;
     }
 
     int rb = 0;   // ring slot of the element row's first node row, (5 r) mod 11
     int rb6 = 0;  // r mod 6
     for (int r = 0; r < maxrows; ++r) {
-      // the row's laminate pairs have landed (its node rows came with the
-      // previous phase); the barrier also ends the previous row's update for
+      // this row's node rows have landed (the phase issued at the previous
+      // row's start); the barrier also ends the previous row's update for
       // every warp, so the ring slots of the previous row's first five node
-      // rows and the update-operand lines are free
-      cp_async_wait_all();
+      // rows are free
+      if (!late) late = !mbar_wait(bar, phase);  // after one timeout, no further waits
+      phase ^= 1u;
       __syncthreads();
       if (kAdj && gpend) {  // previous element row's gradient partials are complete
         double sum = 0.0;
@@ -422,33 +373,33 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         a.grad[a.e_of_g[gpend_e]] -= sum;
         gpend = false;
       }
-      // one phase: the next element row's five new node rows (5r+6 .. 5r+10)
-      // and this row's update operands; waited for before the update
-      if (j == 0)
-        issue_lines<EW>(a, gt, cur, prev, ring, pv, mv, roff, poff, bar, 5 * r + 6, r + 1 < maxrows ? 5 : 0,
-                        rb + 6 >= UR ? rb + 6 - UR : rb + 6, r);
+      // the next element row's five new node rows (5r+6 .. 5r+10)
+      if (j == 0 && r + 1 < maxrows)
+        issue_lines<EW>(a, gt, cur, ring, roff, bar, 5 * r + 6, 5, rb + 6 >= UR ? rb + 6 - UR : rb + 6);
       const bool rowact = r < t_nrows;
       const bool valid = rowact && colok;
       const long long egrid = eg0 + (long long)r * t_nex;
-      if (r + 1 < t_nrows && colok) knext = a.ekeep_g[egrid + t_nex];
+      if (r + 1 < t_nrows && colok) {
+        mnext = a.emat_g[egrid + t_nex];
+        knext = a.ekeep_g[egrid + t_nex];
+      } else {
+        mnext = 0;
+        knext = 0.f;
+      }
       auto slot = [rb](int k) { const int s = rb + k; return s >= UR ? s - UR : s; };
 
       // phase A: row j, xi-derivatives (scaled by 2/ax) to ys
-      if (valid) {
+      {
         const int sj = slot(j);
-        const float* urow = ub + sj * 5 * WP + uoff[sj] + 5 * q;
+        const float* urow = ub + sj * 5 * WP + uoff[sj];
         float2 acc[5][3];
-#pragma unroll
-        for (int f = 0; f < 5; ++f)
-#pragma unroll
-          for (int p = 0; p < 3; ++p) acc[f][p] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < NP; ++k)
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
             const float2 u2 = bc2(urow[f * WP + k]);
 #pragma unroll
-            for (int p = 0; p < 3; ++p) acc[f][p] = fma2(c_Dp[k][p], u2, acc[f][p]);
+            for (int p = 0; p < 3; ++p) acc[f][p] = k == 0 ? mul2(c_Dp[0][p], u2) : fma2(c_Dp[k][p], u2, acc[f][p]);
           }
         const float2 sx2 = bc2(t_sx);
 #pragma unroll
@@ -471,112 +422,106 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       {
         const int i = j;
         float2 Fe2[5][3];
-#pragma unroll
-        for (int f = 0; f < 5; ++f)
-#pragma unroll
-          for (int p = 0; p < 3; ++p) Fe2[f][p] = make_float2(0.f, 0.f);
         float vp = 0.f;
-        if (valid) {
-          float v[5][NP];
+        float v[5][NP];
 #pragma unroll
-          for (int k = 0; k < NP; ++k) {
-            const int sk = slot(k);
-            const float* urow = ub + sk * 5 * WP + uoff[sk] + 5 * q + i;
+        for (int k = 0; k < NP; ++k) {
+          const int sk = slot(k);
+          const float* urow = ub + sk * 5 * WP + uoff[sk] + i;
 #pragma unroll
-            for (int f = 0; f < 5; ++f) v[f][k] = urow[f * WP];
+          for (int f = 0; f < 5; ++f) v[f][k] = urow[f * WP];
+        }
+        // eta-derivatives, packed over node pairs, scaled by 2/ay
+        float2 de2[5][3];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+#pragma unroll
+          for (int m = 0; m < NP; ++m) {
+            const float2 v2 = bc2(v[f][m]);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) de2[f][p] = m == 0 ? mul2(c_Dp[0][p], v2) : fma2(c_Dp[m][p], v2, de2[f][p]);
           }
-          // eta-derivatives, packed over node pairs, scaled by 2/ay
-          float2 de2[5][3];
 #pragma unroll
-          for (int f = 0; f < 5; ++f) {
+          for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
+        }
+        // laminate pairs of the element's material (read-only data cache)
+        const float2* __restrict__ L = a.matp + mcur * LAMP;
+        // the stiffness factor scales the element's fluxes (K_e^0 for the
+        // adjoint); zero for lanes and rows without an element
+        const float akeep = valid ? (kAdj ? t_area4 : t_area4 * keep) : 0.f;
+        // nodes k of the column in blocks of KB: each laminate pair is read
+        // once per block (the products keep their order)
 #pragma unroll
-            for (int p = 0; p < 3; ++p) de2[f][p] = make_float2(0.f, 0.f);
+        for (int k0 = 0; k0 < NP; k0 += KB) {
+          // strains: ex, ey, gxy, kx, ky, kxy, gyz, gxz
+          float sn[KB][8];
 #pragma unroll
-            for (int m = 0; m < NP; ++m) {
-              const float2 v2 = bc2(v[f][m]);
+          for (int kk = 0; kk < KB; ++kk) {
+            const int k = k0 + kk;
+            float gx[5], gy[5];
 #pragma unroll
-              for (int p = 0; p < 3; ++p) de2[f][p] = fma2(c_Dp[m][p], v2, de2[f][p]);
+            for (int f = 0; f < 5; ++f) {
+              gx[f] = ys[f * NPE + i * NP + k];
+              gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
             }
-#pragma unroll
-            for (int p = 0; p < 3; ++p) de2[f][p] = mul2(de2[f][p], bc2(t_sy));
+            sn[kk][0] = gx[0];
+            sn[kk][1] = gy[2];
+            sn[kk][2] = gy[0] + gx[2];
+            sn[kk][3] = gx[1];
+            sn[kk][4] = gy[3];
+            sn[kk][5] = gy[1] + gx[3];
+            sn[kk][6] = v[3][k] + gy[4];
+            sn[kk][7] = v[1][k] + gx[4];
+            if (kSensor) {
+              vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
+            }
           }
-          const float2* L = lsm + lane;  // pair c at L[c * CTA_ELEMS]
-          // the stiffness factor scales the element's fluxes (K_e^0 for the adjoint)
-          const float akeep = kAdj ? t_area4 : t_area4 * keep;
-          // nodes k of the column in blocks of KB: each laminate pair is read
-          // from shared memory once per block (the products keep their order)
+          // R[0] = (Nxx, Nyy), R[1] = (Nxy, Mxx), R[2] = (Myy, Mxy), R[3] = (Qy, Qx)
+          float2 R[4][KB];
 #pragma unroll
-          for (int k0 = 0; k0 < NP; k0 += KB) {
-            // strains: ex, ey, gxy, kx, ky, kxy, gyz, gxz
-            float sn[KB][8];
+          for (int b = 0; b < 3; ++b)
 #pragma unroll
-            for (int kk = 0; kk < KB; ++kk) {
-              const int k = k0 + kk;
-              float gx[5], gy[5];
+            for (int c = 0; c < 6; ++c) {
+              const float2 l = __ldg(L + 6 * b + c);
 #pragma unroll
-              for (int f = 0; f < 5; ++f) {
-                gx[f] = ys[f * NPE + i * NP + k];
-                gy[f] = (k & 1) ? de2[f][k >> 1].y : de2[f][k >> 1].x;
-              }
-              sn[kk][0] = gx[0];
-              sn[kk][1] = gy[2];
-              sn[kk][2] = gy[0] + gx[2];
-              sn[kk][3] = gx[1];
-              sn[kk][4] = gy[3];
-              sn[kk][5] = gy[1] + gx[3];
-              sn[kk][6] = v[3][k] + gy[4];
-              sn[kk][7] = v[1][k] + gx[4];
-              if (kSensor) {
-                vp += a.sc.k0 * (a.sc.e31 * (gx[0] + a.sc.hh * gx[1]) + a.sc.e32 * (gy[2] + a.sc.hh * gy[3]));
-              }
+              for (int kk = 0; kk < KB; ++kk)
+                R[b][kk] = c == 0 ? mul2(l, bc2(sn[kk][c])) : fma2(l, bc2(sn[kk][c]), R[b][kk]);
             }
-            // R[0] = (Nxx, Nyy), R[1] = (Nxy, Mxx), R[2] = (Myy, Mxy), R[3] = (Qy, Qx)
-            float2 R[4][KB];
+          {
+            const float2 l18 = __ldg(L + 18), l19 = __ldg(L + 19);
 #pragma unroll
-            for (int b = 0; b < 3; ++b)
+            for (int kk = 0; kk < KB; ++kk) R[3][kk] = fma2(l19, bc2(sn[kk][7]), mul2(l18, bc2(sn[kk][6])));
+          }
 #pragma unroll
-              for (int c = 0; c < 6; ++c) {
-                const float2 l = L[(6 * b + c) * CTA_ELEMS];
+          for (int kk = 0; kk < KB; ++kk) {
+            const int k = k0 + kk;
+            const float2 NN = R[0][kk], NM = R[1][kk], MM = R[2][kk], QQ = R[3][kk];
+            const float Wn = c_w32[i] * c_w32[k] * akeep;
+            const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
+            // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
+            const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
+            const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
+            const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
+            const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
+            const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
+            const float2 Gs[5] = {G0, G1, G2, G3, G4};
 #pragma unroll
-                for (int kk = 0; kk < KB; ++kk)
-                  R[b][kk] = c == 0 ? mul2(l, bc2(sn[kk][c])) : fma2(l, bc2(sn[kk][c]), R[b][kk]);
-              }
-            {
-              const float2 l18 = L[18 * CTA_ELEMS], l19 = L[19 * CTA_ELEMS];
+            for (int f = 0; f < 5; ++f) {
+              ys[f * NPE + i * NP + k] = Gs[f].x;
+              const float2 ge = bc2(Gs[f].y);
 #pragma unroll
-              for (int kk = 0; kk < KB; ++kk) R[3][kk] = fma2(l19, bc2(sn[kk][7]), mul2(l18, bc2(sn[kk][6])));
+              for (int p = 0; p < 3; ++p) Fe2[f][p] = k == 0 ? mul2(c_DTp[0][p], ge) : fma2(c_DTp[k][p], ge, Fe2[f][p]);
             }
-#pragma unroll
-            for (int kk = 0; kk < KB; ++kk) {
-              const int k = k0 + kk;
-              const float2 NN = R[0][kk], NM = R[1][kk], MM = R[2][kk], QQ = R[3][kk];
-              const float Wn = c_w32[i] * c_w32[k] * akeep;
-              const float2 W2 = mul2(bc2(Wn), wsxy);  // (W*2/ax, W*2/ay)
-              // (Gxi, Geta) per field: Sx = (Nxx, Mxx, Nxy, Mxy, Qx), Sy = (Nxy, Mxy, Nyy, Myy, Qy)
-              const float2 G0 = mul2(W2, make_float2(NN.x, NM.x));
-              const float2 G1 = mul2(W2, make_float2(NM.y, MM.y));
-              const float2 G2 = mul2(W2, make_float2(NM.x, NN.y));
-              const float2 G3 = mul2(W2, make_float2(MM.y, MM.x));
-              const float2 G4 = mul2(W2, make_float2(QQ.y, QQ.x));
-              const float2 Gs[5] = {G0, G1, G2, G3, G4};
-#pragma unroll
-              for (int f = 0; f < 5; ++f) {
-                ys[f * NPE + i * NP + k] = Gs[f].x;
-                const float2 ge = bc2(Gs[f].y);
-#pragma unroll
-                for (int p = 0; p < 3; ++p) Fe2[f][p] = fma2(c_DTp[k][p], ge, Fe2[f][p]);
-              }
-              if (k & 1) {
-                Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
-                Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
-              } else {
-                Fe2[1][k >> 1].x += Wn * QQ.y;
-                Fe2[3][k >> 1].x += Wn * QQ.x;
-              }
+            if (k & 1) {
+              Fe2[1][k >> 1].y += Wn * QQ.y;   // + Sxz.*WWDetJ into mx
+              Fe2[3][k >> 1].y += Wn * QQ.x;   // + Syz.*WWDetJ into my
+            } else {
+              Fe2[1][k >> 1].x += Wn * QQ.y;
+              Fe2[3][k >> 1].x += Wn * QQ.x;
             }
           }
         }
-        if (kSensor && valid) vred[i * CTA_ELEMS + lane] = vp;
+        if (kSensor) vred[i * CTA_ELEMS + lane] = vp;
         if constexpr (kAdj) {
           // column i's share of lambda' K_e^0 u_{n-1} (the row part is added
           // in phase C), then keep_e K_e^0 lambda
@@ -589,11 +534,11 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
                 dl += Fe2[f][p].x * umc[f * a.nnode_pad + (2 * p) * t.NX];
                 dl += Fe2[f][p].y * umc[f * a.nnode_pad + (2 * p + 1) * t.NX];
               }
-#pragma unroll
-            for (int f = 0; f < 5; ++f)
-#pragma unroll
-              for (int p = 0; p < 3; ++p) Fe2[f][p] = mul2(Fe2[f][p], bc2(keep));
           }
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int p = 0; p < 3; ++p) Fe2[f][p] = mul2(Fe2[f][p], bc2(keep));
         }
         // column part at rows m = 0..5 of column i (zeros from lanes without
         // an element, so that stale band values never survive)
@@ -622,48 +567,56 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         }
       }
       __syncthreads();
-      // the next row's laminate pairs replace this row's (read above)
-      if (r + 1 < t_nrows && colok) lam_load(mnext);
-      cp_async_commit();
-      if (r + 2 < t_nrows && colok) mnext = a.emat_g[egrid + 2 * t_nex];
 
-      // phase C: xi-part of the transposed operator, added to the band
-      float out[5][NP];
-      if (valid) {
+      // the update's global loads for band row j, issued before phase C
+      float uo_r[G][NCOL][5], mt_r[G][NCOL], mr_r[G][NCOL];
 #pragma unroll
-        for (int f = 0; f < 5; ++f) {
-          float2 o2[3];
+      for (int gg = 0; gg < G; ++gg) {
+        const bool rok = r >= ulo[gg] && r < uhi[gg];
+        const long long rbase = ub0[gg] + (long long)r * ustr[gg];
 #pragma unroll
-          for (int p = 0; p < 3; ++p) o2[p] = make_float2(0.f, 0.f);
+        for (int s2 = 0; s2 < NCOL; ++s2) {
+          const int c = lane + 32 * s2;
+          if (rok && c < ucol[gg]) {
+            const long long node = rbase + c;
+            mt_r[gg][s2] = a.minv[node];
+            mr_r[gg][s2] = a.minv[a.nnode_pad + node];
 #pragma unroll
-          for (int ii = 0; ii < NP; ++ii) {
-            const float2 gg2 = bc2(ys[f * NPE + ii * NP + j]);
-#pragma unroll
-            for (int p = 0; p < 3; ++p) o2[p] = fma2(c_DTp[ii][p], gg2, o2[p]);
-          }
-#pragma unroll
-          for (int p = 0; p < 3; ++p) {
-            out[f][2 * p] = o2[p].x;
-            out[f][2 * p + 1] = o2[p].y;
+            for (int f = 0; f < 5; ++f) uo_r[gg][s2][f] = prev[f * a.nnode_pad + node];
           }
         }
-        if constexpr (kAdj) {
-          // line j's row part of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
+      }
+      // phase C: xi-part of the transposed operator, added to the band
+      float out[5][NP];
+#pragma unroll
+      for (int f = 0; f < 5; ++f) {
+        float2 o2[3];
+#pragma unroll
+        for (int ii = 0; ii < NP; ++ii) {
+          const float2 gg2 = bc2(ys[f * NPE + ii * NP + j]);
+#pragma unroll
+          for (int p = 0; p < 3; ++p) o2[p] = ii == 0 ? mul2(c_DTp[0][p], gg2) : fma2(c_DTp[ii][p], gg2, o2[p]);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          out[f][2 * p] = o2[p].x;
+          out[f][2 * p + 1] = o2[p].y;
+        }
+      }
+      if constexpr (kAdj) {
+        // line j's row part of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
+        if (valid) {
           const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
 #pragma unroll
           for (int f = 0; f < 5; ++f)
 #pragma unroll
-            for (int i = 0; i < NP; ++i) {
-              dl += out[f][i] * umr[f * a.nnode_pad + i];
-              out[f][i] *= keep;
-            }
+            for (int i = 0; i < NP; ++i) dl += out[f][i] * umr[f * a.nnode_pad + i];
           vred[j * CTA_ELEMS + lane] = dl;
         }
-      } else {
 #pragma unroll
         for (int f = 0; f < 5; ++f)
 #pragma unroll
-          for (int i = 0; i < NP; ++i) out[f][i] = 0.f;
+          for (int i = 0; i < NP; ++i) out[f][i] *= keep;
       }
       // band accumulation: logical row j of this element row is physical row
       // (j - r) mod 6 and already holds the column part (phase B).  Column
@@ -695,20 +648,14 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       if constexpr (!kAdj) {
         // excitation of this band row's owned nodes: the task's forces are
-        // ordered by node row (merged per DOF), warp j walks them with one
-        // cursor per lane group and its lanes subtract a row's entries from
-        // the completed band row (distinct DOFs: no two lanes meet)
+        // ordered by node row (merged per DOF) and indexed by node row, and
+        // the warp's lanes subtract the row's entries from the completed
+        // band row (distinct DOFs: no two lanes meet)
 #pragma unroll
         for (int gg = 0; gg < G; ++gg) {
           const GroupTask& t2 = pick<G>(gt, gg);
           if (t2.fn == 0 || !(r >= ulo[gg] && r < uhi[gg])) continue;
-          const int iy = 5 * (t2.eyA + r) + j;
-          const int fend = t2.f0 + t2.fn;
-          int c0 = fcur[gg];
-          while (c0 < fend && a.f_iy[c0] < iy) ++c0;
-          int c1 = c0;
-          while (c1 < fend && a.f_iy[c1] == iy) ++c1;
-          fcur[gg] = c1;
+          const int c0 = a.f_rowptr[t2.fr0 + 5 * r + j], c1 = a.f_rowptr[t2.fr0 + 5 * r + j + 1];
           if (c1 > c0) {
             const double sv = a.st[(int64_t)t2.scen * a.nft + (nn - 1)];
             float* brow = band + gg * GM::FGS + prow * 5 * W;
@@ -732,9 +679,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           a.vsum[(int64_t)sl * a.nft + (nn - 1)] = sum;
         }
       }
-      // this row's update operands (and the next row's node rows) have landed
-      if (!late) late = !mbar_wait(bar, phase);
-      phase ^= 1u;
       // update owned, complete nodes of band row j (excitation subtracted
       // above by the node's owner)
 #pragma unroll
@@ -743,11 +687,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         const long long rowbase = ub0[gg] + (long long)r * ustr[gg];
         const float* urow = ring + gg * GM::UGS + slot(j) * 5 * WP + roff[gg * UR + slot(j)] + 5;
         const float* bnd = band + gg * GM::FGS + prow * 5 * W + 5;
-        // u_{n-1} and 1/M from the phase's lines (node rows 0..4 of the band);
-        // the plate's top node row (j == 5) reads them from global memory
-        const int po = j < 5 ? poff[gg * 5 + j] : 0;
-        const float* pvr = pv + gg * GM::PVS + (j < 5 ? j : 0) * 5 * GM::OWNP + po;
-        const float* mvr = mv + gg * GM::MVS + (j < 5 ? j : 0) * 2 * GM::OWNP + po;
         const GroupTask& t2 = pick<G>(gt, gg);
 #pragma unroll
         for (int s = 0; s < NCOL; ++s) {
@@ -768,19 +707,11 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
               }
           }
           if (!kAdj && a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, node);
-          float mt, mr;
-          if (j < 5) {
-            mt = mvr[c];
-            mr = mvr[GM::OWNP + c];
-          } else {
-            mt = a.minv[node];
-            mr = a.minv[a.nnode_pad + node];
-          }
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
             const float u = urow[f * WP + c];
-            const float uo = j < 5 ? pvr[f * GM::OWNP + c] : prev[f * a.nnode_pad + node];
-            const float im = (f == 1 || f == 3) ? mr : mt;
+            const float uo = uo_r[gg][s][f];
+            const float im = (f == 1 || f == 3) ? mr_r[gg][s] : mt_r[gg][s];
             const float un = u + a.k1[f] * (u - uo) - a.k2[f] * (im * F[f]);
             dst[f * a.nnode_pad + node] = un;
             if (frame) store_frame(a.fs, a.frames, a.nnode_pad, node, f, nn, u, uo, un, a.a0, a.a1);
@@ -790,12 +721,12 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       }
       // (the next row's first barrier separates this update from the ring
       // refill and the next band accumulation)
+      mcur = mnext;
       keep = knext;
       rb += 5;
       if (rb >= UR) rb -= UR;
       if (++rb6 == 6) rb6 = 0;
     }
-    cp_async_wait_all();
     __syncthreads();
     if (kAdj && gpend) {  // the task's last element row
       double sum = 0.0;

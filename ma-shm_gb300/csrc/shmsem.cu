@@ -336,7 +336,7 @@ struct StructPlan {
   int* emat_g = nullptr;
   void* ekeep_g = nullptr;
   int* esens_g = nullptr;
-  int *f_xl = nullptr, *f_iy = nullptr, *f_field = nullptr;
+  int *f_xl = nullptr, *f_iy = nullptr, *f_field = nullptr, *f_rowptr = nullptr;
   double* f_val = nullptr;
   int *o_xl = nullptr, *o_iy = nullptr, *o_field = nullptr, *o_q = nullptr;  // point outputs per task
   int* e_of_g = nullptr;   // grid-order element -> plan element
@@ -780,7 +780,7 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     for (int b = 0; b < nb; ++b)
       for (int k = 0; k < ns; ++k) {
         TaskTmp t;
-        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0};  // rows, forces and outputs set below
+        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0, -1};  // rows, forces and outputs set below
         const int last = std::min(H * (b + 1), pl.ney);
         t.t.nrows = b == 0 ? last : last - (H * b - 1);
         task_index[s][(size_t)b * ns + k] = (int)tasks.size();
@@ -848,7 +848,7 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
   // longest tasks first so that lane groups of a CTA stay in step
   std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
   std::vector<TaskDesc> td;
-  std::vector<int> fxl, fiy, ffield, oxl, oiy, ofield, oq;
+  std::vector<int> fxl, fiy, ffield, oxl, oiy, ofield, oq, frp;
   std::vector<double> fval;
   for (TaskTmp& t : tasks) {
     t.t.o0 = (int)oxl.size();
@@ -859,6 +859,16 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     oq.insert(oq.end(), t.oq.begin(), t.oq.end());
     t.t.f0 = (int)fxl.size();
     t.t.fn = (int)t.fxl.size();
+    if (t.t.fn > 0) {  // node-row pointers: entries of task node row k are [frp[k], frp[k+1])
+      const int iy0 = 5 * (t.t.block == 0 ? 0 : t.t.block * H - 1);
+      const int nr = 5 * t.t.nrows + 1;
+      t.t.fr0 = (int)frp.size();
+      size_t k = 0;
+      for (int row = 0; row <= nr; ++row) {
+        while (k < t.fiy.size() && t.fiy[k] - iy0 < row) ++k;
+        frp.push_back(t.t.f0 + (int)k);
+      }
+    }
     fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
     fiy.insert(fiy.end(), t.fiy.begin(), t.fiy.end());
     ffield.insert(ffield.end(), t.ffield.begin(), t.ffield.end());
@@ -879,11 +889,12 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
   if ((st = upload(p, &sp.f_iy, fiy)) != SHM_OK) return st;
   if ((st = upload(p, &sp.f_field, ffield)) != SHM_OK) return st;
   if ((st = upload(p, &sp.f_val, fval)) != SHM_OK) return st;
+  if ((st = upload(p, &sp.f_rowptr, frp)) != SHM_OK) return st;
   if ((st = upload(p, &sp.o_xl, oxl)) != SHM_OK) return st;
   if ((st = upload(p, &sp.o_iy, oiy)) != SHM_OK) return st;
   if ((st = upload(p, &sp.o_field, ofield)) != SHM_OK) return st;
   if ((st = upload(p, &sp.o_q, oq)) != SHM_OK) return st;
-  sp.task_allocs = {dt, sp.f_xl, sp.f_iy, sp.f_field, sp.f_val, sp.o_xl, sp.o_iy, sp.o_field, sp.o_q};
+  sp.task_allocs = {dt, sp.f_xl, sp.f_iy, sp.f_field, sp.f_val, sp.f_rowptr, sp.o_xl, sp.o_iy, sp.o_field, sp.o_q};
   sp.tasks = dt;
   sp.ntask = (int)td.size();
   sp.tile = EW;
@@ -1027,6 +1038,7 @@ static F32Args struct_f32_args(shm_plan* p) {
   a.esens_g = sp.esens_g;
   a.f_xl = sp.f_xl;
   a.f_iy = sp.f_iy;
+  a.f_rowptr = sp.f_rowptr;
   a.f_field = sp.f_field;
   a.f_val = sp.f_val;
   a.st = p->st;
