@@ -78,35 +78,6 @@ __device__ __forceinline__ void store_frame(const FrameSpec& fs, T* __restrict__
   if (sA >= 0) base[sA * npad] = a0 * (uo - T(2) * u + un);
 }
 
-// Sum of one node's element copies, F[f] += F2[f * plane + slots[s]] for
-// s = s0 .. s1-1 in that order (the basket order, so results do not change):
-// the first KMAX slot indices and then their values are all loaded before the
-// first sum, so the node's gathers are in flight together instead of one
-// dependent pair at a time; longer lists continue slot by slot.
-template <typename T, int NF, int KMAX>
-__device__ __forceinline__ void gather_slots(const int* __restrict__ slots, const T* __restrict__ F2, int64_t plane,
-                                             int s0, int s1, T (&F)[NF]) {
-  int sl[KMAX];
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k) sl[k] = s0 + k < s1 ? slots[s0 + k] : 0;
-  T v[NF][KMAX];
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k)
-#pragma unroll
-    for (int f = 0; f < NF; ++f) v[f][k] = s0 + k < s1 ? F2[f * plane + sl[k]] : T(0);
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k)
-    if (s0 + k < s1) {
-#pragma unroll
-      for (int f = 0; f < NF; ++f) F[f] += v[f][k];
-    }
-  for (int s = s0 + KMAX; s < s1; ++s) {
-    const int64_t slot = slots[s];
-#pragma unroll
-    for (int f = 0; f < NF; ++f) F[f] += F2[f * plane + slot];
-  }
-}
-
 // Pressure loading: nodal frames pf[k][node_pad], lumped area parea[node],
 // per step (row nn-1 of pcoef) the two frames and their weights
 // {f0, f1, c0, c1}; the load on w is parea * (c0 pf[f0] + c1 pf[f1]).

@@ -48,7 +48,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 // (Qy,Qx):   (a44,a45) (a45,a55)
 constexpr int LAMP = 20;
 #ifndef SHM_F32_KB
-#define SHM_F32_KB 3
+#define SHM_F32_KB 6
 #endif
 constexpr int KB = SHM_F32_KB;  // column nodes per laminate read in phase B (divides 6)
 static_assert(NP % KB == 0, "laminate blocks cover the column");
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         gpend = false;
       }
       // the next element row's five new node rows (5r+6 .. 5r+10)
-      if (j == 0 && r + 1 < maxrows)
+      if (j == 5 && r + 1 < maxrows)  // warp 5: it has no band row to update in most rows
         issue_lines<EW>(a, gt, cur, ring, roff, bar, 5 * r + 6, 5, rb + 6 >= UR ? rb + 6 - UR : rb + 6);
       const bool rowact = r < t_nrows;
       const bool valid = rowact && colok;

@@ -265,7 +265,11 @@ __global__ void __launch_bounds__(256) k_node_general(GenArgs<T> a, int kstep) {
   const T* __restrict__ cur = odd ? a.UB : a.UA;
   T* prev = odd ? a.UA : a.UB;
   T F[5] = {T(0), T(0), T(0), T(0), T(0)};
-  gather_slots<T, 5, 4>(a.slots, a.F2, a.plane, a.row_ptr[g], a.row_ptr[g + 1], F);
+  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
   if (a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, g);
   T* dst = a.outp ? a.outp : prev;
   const T mt = a.minv[g], mr = a.minv[a.nnode_pad + g];
@@ -293,7 +297,11 @@ __global__ void k_assemble_only(GenArgs<T> a, T* out) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= a.nnode) return;
   T F[5] = {T(0), T(0), T(0), T(0), T(0)};
-  gather_slots<T, 5, 4>(a.slots, a.F2, a.plane, a.row_ptr[g], a.row_ptr[g + 1], F);
+  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
 #pragma unroll
   for (int f = 0; f < 5; ++f) out[f * a.nnode_pad + g] = F[f];
 }

@@ -241,7 +241,11 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
   const T* __restrict__ cur = odd ? a.UB : a.UA;
   T* prev = odd ? a.UA : a.UB;
   T F[3] = {T(0), T(0), T(0)};
-  gather_slots<T, 3, 8>(a.slots, a.F2, a.plane, a.row_ptr[g], a.row_ptr[g + 1], F);
+  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
+    const int64_t slot = a.slots[s];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) F[f] += a.F2[f * a.plane + slot];
+  }
   const T im = a.minv[g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
   const bool guard = guard_step(a.fs, nn);
