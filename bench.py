@@ -267,8 +267,9 @@ def adjoint_record(pkg, maps=64, steps=20000, check_steps=2000, nfd=20):
     """Config 5 reduced to what fits the default run: gradient cost / forward
     cost on the full damage-identification batch (64 maps, 50x50 elements,
     20 000 steps, checkpoints every 200, FP32 structured plan) with the state
-    store at its default (half the free memory) and off (every segment
-    recomputed); gradient accuracy on map 0 over the first `check_steps`
+    store at its default (half the free memory), off (every segment
+    recomputed) and at the opt-in setting (the free memory less 8 GiB);
+    gradient accuracy on map 0 over the first `check_steps`
     steps: FP32 and FP64 adjoint gradients against central differences of the
     FP64 forward on `nfd` random parameters (all 2 nfd perturbed plates in
     one batched plan)."""
@@ -290,7 +291,7 @@ def adjoint_record(pkg, maps=64, steps=20000, check_steps=2000, nfd=20):
         torch.cuda.synchronize()
         t_fwd = time.perf_counter() - t0
         out["forward_s"] = t_fwd
-        for label, cap in (("store_default", None), ("store_off", 0)):
+        for label, cap in (("store_default", None), ("store_off", 0), ("store_spare", "spare")):
             p.set_adjoint_store(cap)
             t0 = time.perf_counter()
             p.forward_backward(targets, ckpt_every=200)
