@@ -32,13 +32,12 @@ ALG_BYTES = {32: 16.0, 64: 32.0}   # algorithmic bytes per DOF-step (u_n, u_n-1,
 # DRAM bytes (read + write) per DOF of one k_struct_step_f32 launch (tile 32), from an
 # ncu capture of one launch on the 64-plate batch (294.1 + 81.1 MB for 30 001 270 DOF;
 # the profile summary of k_struct_step_f32 under profiles/); traffic grows with the DOF count
-F32_TRAFFIC_PER_DOF = (294.067712e6 + 81.064192e6) / 30001270
-# floating-point operations per DOF-step of k_struct_step_f32, counted by ncu on the
-# same launch of the v6 build (sm__sass_thread_inst_executed_op_*: 706.5 M FFMA2 x 4,
-# 170.4 M FMUL2 x 2, 78.6 M FFMA x 2, 48.8 M FMUL, 82.9 M FADD) over 30 001 270 DOF; the
-# current build applies the stiffness factor once per line instead of to the 20 staged
-# laminate pairs (0.3 % fewer products), the other operations are unchanged
-F32_FLOP_PER_DOF = (706.536432e6 * 4 + 170.43642e6 * 2 + 78.595604e6 * 2 + 48.797086e6 + 82.893812e6) / 30001270
+F32_TRAFFIC_PER_DOF = (292.645632e6 + 80.066048e6) / 30001270
+# floating-point operations per DOF-step executed by k_struct_step_f32, counted by ncu on
+# the same launch (sass__thread_inst_executed_true_per_opcode: 740.6 M FFMA2 x 4, 280.5 M
+# FMUL2 x 2, 82.4 M FFMA x 2, 54.7 M FMUL, 147.9 M FADD) over 30 001 270 DOF; lanes without
+# an element execute the same instructions on zeros, so this exceeds the useful count
+F32_FLOP_PER_DOF = (740.55168e6 * 4 + 280.512e6 * 2 + 82.4435e6 * 2 + 54.743158e6 + 147.884554e6) / 30001270
 METRIC = "DOF-steps/s (batched flat-shell SEM forward, 512 uneven plates)"
 
 
