@@ -28,11 +28,12 @@ struct PlateDesc {
 
 // task: plate, strip, block, rows, first force entry, force count, first
 // point-output entry, point-output count (the outputs the task's update owns),
-// and for tasks with forces the offset of their node-row pointer table
+// and the offsets of the forces' and the outputs' node-row pointer tables
+// (-1 for a task without them)
 struct TaskDesc {
   int plate, strip, block, nrows;
   int f0, fn, o0, on;
-  int fr0;
+  int fr0, or0;
 };
 
 template <typename T> struct StructArgs {

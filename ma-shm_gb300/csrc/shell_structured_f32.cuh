@@ -151,7 +151,7 @@ struct F32Args {
   const int* __restrict__ esens_g;
   const int* __restrict__ f_xl;
   const int* __restrict__ f_iy;
-  const int* __restrict__ f_rowptr;  // per task with forces: first entry of each node row (5 nrows + 2)
+  const int* __restrict__ f_rowptr;  // node-row pointer tables of the task force and output lists
   const int* __restrict__ f_field;
   const double* __restrict__ f_val;
   const double* __restrict__ st;
@@ -180,7 +180,7 @@ struct F32Args {
 
 // per-group task facts, uniform inside the group
 struct GroupTask {
-  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, fr0, scen, o0, on;
+  int has, nrows, eyA, block, strip, plate, ney, nex, NX, f0, fn, fr0, scen, o0, on, or0;
   long long node0, egrid0;
   float sx, sy, area4;
 };
@@ -204,6 +204,7 @@ __device__ __forceinline__ GroupTask load_group_task(const F32Args& a, int tid) 
   t.fr0 = tk.fr0;
   t.o0 = tk.o0;
   t.on = tk.on;
+  t.or0 = tk.or0;
   t.scen = pl.scen;
   t.node0 = pl.node0;
   t.egrid0 = pl.egrid0;
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         double sum = 0.0;
 #pragma unroll
         for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
-        a.grad[a.e_of_g[gpend_e]] -= sum;
+        atomicAdd(&a.grad[a.e_of_g[gpend_e]], -sum);  // one thread per element: no waiting on a read
         gpend = false;
       }
       // the next element row's five new node rows (5r+6 .. 5r+10)
@@ -664,6 +665,23 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
             __syncwarp();
           }
         }
+      } else {
+        // the adjoint's residual forces at the point outputs of this band row
+        // (a few entries: one lane adds them in list order)
+#pragma unroll
+        for (int gg = 0; gg < G; ++gg) {
+          const GroupTask& t2 = pick<G>(gt, gg);
+          if (t2.on == 0 || !(r >= ulo[gg] && r < uhi[gg])) continue;
+          const int c0 = a.f_rowptr[t2.or0 + 5 * r + j], c1 = a.f_rowptr[t2.or0 + 5 * r + j + 1];
+          if (c1 > c0) {
+            if (lane == 0) {
+              float* brow = band + gg * GM::FGS + prow * 5 * W;
+              for (int oi = c0; oi < c1; ++oi)
+                brow[a.o_field[oi] * W + a.o_xl[oi]] += (float)a.asig[(int64_t)a.o_q[oi] * a.nft + (nn - 1)];
+            }
+            __syncwarp();
+          }
+        }
       }
       const bool owned_row = rowact && (t.block == 0 || r > 0);
       if (kAdj && j == 0) {  // reduced after the next CTA barrier
@@ -687,7 +705,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
         const long long rowbase = ub0[gg] + (long long)r * ustr[gg];
         const float* urow = ring + gg * GM::UGS + slot(j) * 5 * WP + roff[gg * UR + slot(j)] + 5;
         const float* bnd = band + gg * GM::FGS + prow * 5 * W + 5;
-        const GroupTask& t2 = pick<G>(gt, gg);
 #pragma unroll
         for (int s = 0; s < NCOL; ++s) {
           const int c = lane + 32 * s;
@@ -696,16 +713,6 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
           float F[5];
 #pragma unroll
           for (int f = 0; f < 5; ++f) F[f] = bnd[f * W + c];
-          if (kAdj && t2.on > 0) {
-            const int iy = 5 * (t2.eyA + r) + j;
-            for (int oi = t2.o0; oi < t2.o0 + t2.on; ++oi)
-              if (a.o_iy[oi] == iy && a.o_xl[oi] == 5 + c) {
-                const float rv = (float)a.asig[(int64_t)a.o_q[oi] * a.nft + (nn - 1)];
-#pragma unroll
-                for (int f = 0; f < 5; ++f)
-                  if (f == a.o_field[oi]) F[f] += rv;
-              }
-          }
           if (!kAdj && a.pr.npf > 0) F[4] -= pressure_load(a.pr, nn, a.nnode_pad, node);
 #pragma unroll
           for (int f = 0; f < 5; ++f) {
@@ -732,7 +739,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
       double sum = 0.0;
 #pragma unroll
       for (int i = 0; i < NP; ++i) sum += (double)vred[i * CTA_ELEMS + lane];
-      a.grad[a.e_of_g[gpend_e]] -= sum;
+      atomicAdd(&a.grad[a.e_of_g[gpend_e]], -sum);
       gpend = false;
     }
   }

@@ -788,7 +788,7 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     for (int b = 0; b < nb; ++b)
       for (int k = 0; k < ns; ++k) {
         TaskTmp t;
-        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0, -1};  // rows, forces and outputs set below
+        t.t = TaskDesc{s, k, b, 0, 0, 0, 0, 0, -1, -1};  // rows, forces and outputs set below
         const int last = std::min(H * (b + 1), pl.ney);
         t.t.nrows = b == 0 ? last : last - (H * b - 1);
         task_index[s][(size_t)b * ns + k] = (int)tasks.size();
@@ -853,30 +853,57 @@ static shm_status struct_tasks(shm_plan* p, int EW, int H) {
     t.ffield.swap(fld);
     t.fval.swap(val);
   }
+  // each task's point outputs ordered by node row, then column (stable: the
+  // entries of one DOF keep their order)
+  for (TaskTmp& t : tasks) {
+    const size_t n = t.oxl.size();
+    if (n < 2) continue;
+    std::vector<size_t> ord(n);
+    for (size_t i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+      return t.oiy[a] != t.oiy[b] ? t.oiy[a] < t.oiy[b] : t.oxl[a] < t.oxl[b];
+    });
+    std::vector<int> xl(n), iy(n), fld(n), oq(n);
+    for (size_t i = 0; i < n; ++i) {
+      xl[i] = t.oxl[ord[i]];
+      iy[i] = t.oiy[ord[i]];
+      fld[i] = t.ofield[ord[i]];
+      oq[i] = t.oq[ord[i]];
+    }
+    t.oxl.swap(xl);
+    t.oiy.swap(iy);
+    t.ofield.swap(fld);
+    t.oq.swap(oq);
+  }
   // longest tasks first so that lane groups of a CTA stay in step
   std::stable_sort(tasks.begin(), tasks.end(), [](const TaskTmp& a, const TaskTmp& b) { return a.t.nrows > b.t.nrows; });
   std::vector<TaskDesc> td;
   std::vector<int> fxl, fiy, ffield, oxl, oiy, ofield, oq, frp;
   std::vector<double> fval;
+  // node-row pointers of a task's sorted list: the entries of task node row k
+  // (node row 5 eyA + k) are [frp[r0 + k], frp[r0 + k + 1]), k = 0 .. 5 nrows
+  auto row_pointers = [&](const TaskDesc& td_, const std::vector<int>& iys, int first) {
+    const int iy0 = 5 * (td_.block == 0 ? 0 : td_.block * H - 1);
+    const int nr = 5 * td_.nrows + 1;
+    const int r0 = (int)frp.size();
+    size_t k = 0;
+    for (int row = 0; row <= nr; ++row) {
+      while (k < iys.size() && iys[k] - iy0 < row) ++k;
+      frp.push_back(first + (int)k);
+    }
+    return r0;
+  };
   for (TaskTmp& t : tasks) {
     t.t.o0 = (int)oxl.size();
     t.t.on = (int)t.oxl.size();
+    if (t.t.on > 0) t.t.or0 = row_pointers(t.t, t.oiy, t.t.o0);
     oxl.insert(oxl.end(), t.oxl.begin(), t.oxl.end());
     oiy.insert(oiy.end(), t.oiy.begin(), t.oiy.end());
     ofield.insert(ofield.end(), t.ofield.begin(), t.ofield.end());
     oq.insert(oq.end(), t.oq.begin(), t.oq.end());
     t.t.f0 = (int)fxl.size();
     t.t.fn = (int)t.fxl.size();
-    if (t.t.fn > 0) {  // node-row pointers: entries of task node row k are [frp[k], frp[k+1])
-      const int iy0 = 5 * (t.t.block == 0 ? 0 : t.t.block * H - 1);
-      const int nr = 5 * t.t.nrows + 1;
-      t.t.fr0 = (int)frp.size();
-      size_t k = 0;
-      for (int row = 0; row <= nr; ++row) {
-        while (k < t.fiy.size() && t.fiy[k] - iy0 < row) ++k;
-        frp.push_back(t.t.f0 + (int)k);
-      }
-    }
+    if (t.t.fn > 0) t.t.fr0 = row_pointers(t.t, t.fiy, t.t.f0);
     fxl.insert(fxl.end(), t.fxl.begin(), t.fxl.end());
     fiy.insert(fiy.end(), t.fiy.begin(), t.fiy.end());
     ffield.insert(ffield.end(), t.ffield.begin(), t.ffield.end());

@@ -12,7 +12,12 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-10
 FP32_TOL = 1e-3
-FP32_VOLT_TOL = 5e-3
+# The PZT voltage is a strain measure.  On the batch test's sensor (three
+# elements at the plates' lower edge, which the wave has barely reached after
+# 400 steps) the signal is small and FP32 rounding shows most: measured 1.44e-3
+# there, against 1.1e-7 on the multi-PZT plate and 5.5e-6 on the 200x200-element
+# PZT plate, whose sensors sit in the wave's path.
+FP32_VOLT_TOL = 2e-3
 
 
 def rel(a, b):
@@ -207,7 +212,9 @@ def test_packed_fp32_kernel_matches_oracle(pkg, tile):
             for key in ("displ", "frames"):
                 assert rel(res[path][s][key], ref[key]) <= FP32_TOL, (path, s, key)
             # the PZT voltage is a strain measure read as the wave front
-            # arrives; FP32 state error shows up more there than on displacements
+            # arrives; FP32 state error shows up more there than on
+            # displacements (measured up to 3.6e-6 on displacements and 1.1e-5
+            # on frames here, 1.44e-3 on this sensor's voltage)
             assert rel(res[path][s]["voltage"], ref["voltage"]) <= FP32_VOLT_TOL, (path, s)
         assert rel(res[2][s]["displ"], res[3][s]["displ"]) <= 1e-4
 
@@ -413,8 +420,8 @@ def test_multi_pzt_actuator_and_sensors_match_oracle(pkg, precision, path, rando
     if precision == 64:
         assert rel(got["voltage"], ref["voltage"]) <= FP64_TOL
         assert rel(got["displ"], ref["displ"]) <= FP64_TOL
-    else:
-        assert rel(got["voltage"], ref["voltage"]) <= FP32_VOLT_TOL
+    else:  # measured 1.1e-7 (voltage) and 1.7e-6 (displacement)
+        assert rel(got["voltage"], ref["voltage"]) <= FP32_TOL
         assert rel(got["displ"], ref["displ"]) <= FP32_TOL
 
 
@@ -454,7 +461,9 @@ def test_all_frame_fields_match_oracle(pkg, precision, path):
     plan.close()
     _, ref = oracle_run(scs[0], run)
     assert got.shape == ref["frames"].shape
-    tols = (FP64_TOL,) * 3 if precision == 64 else (FP32_TOL, FP32_TOL, 1e-2)
+    # FP32 measured: displacement 2.3e-6, velocity 5.3e-6, acceleration 1.2e-4
+    # (structured) and 1.4e-4 (general path)
+    tols = (FP64_TOL,) * 3 if precision == 64 else (FP32_TOL, FP32_TOL, FP32_TOL)
     for kind in range(3):
         sl = slice(5 * kind, 5 * kind + 5)
         assert np.abs(ref["frames"][:, sl]).max() > 0
