@@ -470,6 +470,18 @@ def single_plate_bench(pkg, args):
         out[f"fp{prec}_dof_steps_per_s"] = ndof * nsteps / dt
         out[f"fp{prec}_s"] = dt
         out[f"fp{prec}_path"] = p.info["path"]
+        if prec == 32 and p.info["path"] == 2 and args.workload != "solid":
+            # the launch mode the autotuner did not keep, on the same tasks
+            mode = bool(p.info["persistent"])
+            p.set_persistent(not mode)
+            p.forward(want_frames=run.frm_int > 0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r2 = p.forward(want_frames=run.frm_int > 0)[0]
+            torch.cuda.synchronize()
+            dt2 = time.perf_counter() - t0
+            out["fp32_other_launch_mode"] = {"persistent": not mode, "dof_steps_per_s": ndof * nsteps / dt2,
+                                             "same_bits": bool(np.array_equal(r2["displ"], r["displ"]))}
         p.close()
     def rel(a, b):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
@@ -536,6 +548,9 @@ def main():
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--persistent", type=int, default=-1, choices=(-1, 0, 1),
+                    help="structured FP32 plans: -1 as the autotuner chose (off without it), 0 per-step "
+                         "launches in CUDA graphs, 1 one persistent launch per advance")
     ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general, 2 structured, 3 structured generic")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -606,9 +621,12 @@ def main():
         t0 = time.perf_counter()
         tuned = plan.autotune(10)
         setup["autotune_s"] = time.perf_counter() - t0
+    if args.persistent >= 0 and plan.info["path"] == 2 and args.precision == 32:
+        plan.set_persistent(bool(args.persistent))
     config["path"] = "general" if plan.info["path"] == 1 else "structured"
     config["tile_elems"] = plan.info["tile"]
     config["rows_per_block"] = plan.info["rows_per_block"]
+    config["persistent"] = bool(plan.info["persistent"])
     config["autotuned"] = tuned is not None
     plan.reset()
     plan.set_signal()
@@ -636,9 +654,12 @@ def main():
             "fp32_tflops": (F32_FLOP_PER_DOF * value / 1e12 if args.precision == 32 and plan.info["path"] == 2
                             else None),
             "flop_per_dof_step": F32_FLOP_PER_DOF if args.precision == 32 else None,
-            "basis": f"{ALG_BYTES[args.precision]:.0f} B/DOF-step x {ndof} DOF per launch of "
-                     f"k_struct_step, CUDA events over {args.steps} launches; peak {pk_kind}"}
-    launches = args.steps * plan.info["launches_per_step"] + (args.steps // args.graph if args.graph else 1)
+            "basis": f"{ALG_BYTES[args.precision]:.0f} B/DOF-step x {ndof} DOF per step of "
+                     f"the fused structured step, CUDA events over {args.steps} steps; peak {pk_kind}"}
+    if plan.info["persistent"]:
+        launches = 2   # the persistent step kernel and the step-counter kernel
+    else:
+        launches = args.steps * plan.info["launches_per_step"] + (args.steps // args.graph if args.graph else 1)
 
     e2e = None
     r32 = None

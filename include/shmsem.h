@@ -155,7 +155,8 @@ shm_status shm_apply_stiffness(shm_plan *plan, const double *U, double *F);
 
 /* Plan facts: [0] total nodes, [1] total elements, [2] total DOF, [3] path
  * used (1 general, 2 structured), [4] precision, [5] frames per scenario,
- * [6] kernel launches per step, [7] tile elements (structured), [8] rows per task,
+ * [6] kernel launches per step (0: persistent, one launch per advance), [7] tile
+ * elements (structured), [8] rows per task,
  * [9] fields per frame. */
 shm_status shm_plan_info(const shm_plan *plan, int64_t *info10);
 
@@ -222,10 +223,29 @@ shm_status shm_set_adjoint_store(shm_plan *plan, int64_t max_bytes, int32_t *las
  * task) candidate of the structured kernel -- {16, 32} x {4, 8, 16, 32, 64,
  * and per width the fewest rows that keep all tasks within one and within
  * two waves of two CTAs per SM} -- re-planning the task list each time, keeps
- * the fastest and resets the state.  Returns the choice (tile_elems = 0: general kernels) and its ms per
- * step. */
+ * the fastest and resets the state.  On FP32 plans each structured candidate
+ * is timed both as graph-chunked launches and as a persistent launch
+ * (shm_set_persistent); the faster mode is kept (shm_plan_info [6] = 0 when
+ * persistent).  Returns the choice (tile_elems = 0: general kernels) and its
+ * ms per step. */
 shm_status shm_autotune(shm_plan *plan, int32_t steps, int32_t *tile_elems, int32_t *rows_per_block,
                         float *ms_per_step);
+
+/* Persistent stepping.  The reference launches its gpuArray operations one
+ * by one for every step (main_flat_shell.m:651-917); by default the engine
+ * launches one fused kernel per step, chunked into CUDA graphs.  With
+ * enable = 1 an FP32 plan on the structured fused kernel advances all the
+ * steps of an shm_advance / shm_forward call in ONE cooperative launch whose
+ * CTAs stay resident and meet at a device-wide barrier between steps (the
+ * grid is at most the number of co-resident CTAs; each CTA takes the same
+ * task groups every step).  This removes the per-step launch gap that
+ * dominates small plates.  Results are bit-identical to the per-step
+ * launches.  spin_limit bounds each barrier wait (polls of ~32 ns; < 0 =
+ * default 2^22): a wait that runs out makes every CTA leave at its next
+ * barrier and the call return SHM_ERR_TIMEOUT.  Returns SHM_ERR_BAD_ARG for a
+ * plan that is not FP32 structured, SHM_ERR_UNSUPPORTED when the device has
+ * no cooperative launch.  enable = 0 restores per-step launches. */
+shm_status shm_set_persistent(shm_plan *plan, int32_t enable, int32_t spin_limit);
 
 /* Diagonal mass vector of the plan (reference mg before scaling, :493-501),
  * [total_nodes x 5] interleaved. */

@@ -258,8 +258,16 @@ __device__ __forceinline__ void issue_lines(const F32Args& a, const GroupTask* g
 // place of u, residual forces r(n) at the point outputs instead of the
 // excitation, and dJ/dd_e -= lambda_n' K_e^0 u_{n-1} accumulated per element
 // (FP32 line products, FP64 per-element and across-step sums).
-template <int EW, bool kSensor, bool kAdj = false>
-__global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, int kstep) {
+//
+// One time step of every task the CTA takes (tasks blockIdx.x, + gridDim.x,
+// ...).  `bar` is the CTA's initialised mbarrier and `phase` the parity of its
+// next phase: both persist across calls, so a persistent kernel can run many
+// steps on one mbarrier.  reuse: the CTA takes the same single task group as
+// in its previous call, whose task facts and ring padding are still in shared
+// memory.
+template <int EW, bool kSensor, bool kAdj>
+__device__ __forceinline__ void struct_f32_step(const F32Args& a, int kstep, unsigned bar, unsigned& phase,
+                                                bool reuse = false) {
   using GM = F32Geom<EW>;
   using SM = F32Smem<EW>;
   constexpr int G = GM::G;
@@ -274,19 +282,19 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   float* edge = sm + SM::EDGE;
   float* ring = sm + SM::RING;
   float* band = sm + SM::BAND;
-  __shared__ __align__(8) unsigned long long bar_mem;
   __shared__ int roff[G * UR];  // ring slot -> smem offset of relative column 0
   __shared__ GroupTask gt[G];   // task facts of the lane groups (shared, not in registers)
-  const unsigned bar = smem_u32(&bar_mem);
 
   const int nn = *a.d_base + kstep;
   const bool odd = ((nn - a.nn_first) & 1);
-  const float* __restrict__ cur = odd ? a.UB : a.UA;
+  const float* cur = odd ? a.UB : a.UA;
   float* prev = odd ? a.UA : a.UB;
   float* dst = a.outp ? a.outp : prev;
+  // (read through L2: in a persistent launch other CTAs wrote these words
+  // in the previous step, and this SM's L1 may hold an older copy)
   if (blockIdx.x == 0)
     for (int q = threadIdx.x; q < a.nout; q += blockDim.x)
-      a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)cur[a.out_field[q] * a.nnode_pad + a.out_node[q]];
+      a.displ[(int64_t)q * a.nft + (nn - 1)] = (double)__ldcg(cur + a.out_field[q] * a.nnode_pad + a.out_node[q]);
 
   const int j = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -297,18 +305,24 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   const bool guard = guard_step(a.fs, nn);
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false, late = false;
-  unsigned phase = 0;      // parity of the mbarrier phase to wait for next
   bool gpend = false;      // adjoint: an element's gradient partials await reduction
   long long gpend_e = 0;   // (its grid-order index)
-  if (threadIdx.x == 0) mbar_init(bar, 1);
 
   for (int tg = blockIdx.x; tg < ntg; tg += gridDim.x) {
     __syncthreads();
-    if (threadIdx.x < G) gt[threadIdx.x] = load_group_task(a, tg * G + threadIdx.x);
-    // columns that no copy of this task writes stay finite (lanes without an
-    // element read them)
-    for (int i = threadIdx.x; i < G * GM::UGS; i += blockDim.x) ring[i] = 0.f;
-    for (int i = threadIdx.x; i < G * GM::FGS; i += blockDim.x) band[i] = 0.f;
+    if (!reuse) {
+      if (threadIdx.x < G) gt[threadIdx.x] = load_group_task(a, tg * G + threadIdx.x);
+      // columns that no copy of this task writes stay finite (lanes without
+      // an element read them); the copies write the same columns every step
+      for (int i = threadIdx.x; i < G * GM::UGS; i += blockDim.x) ring[i] = 0.f;
+      // the bulk copies (async proxy) write ring words just zeroed through
+      // the generic proxy: order the two
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    // band row 0 is the one the first element row adds to (the column part
+    // of the others is stored, not added)
+    for (int g2 = 0; g2 < G; ++g2)
+      for (int i = threadIdx.x; i < 5 * GM::W; i += blockDim.x) band[g2 * GM::FGS + i] = 0.f;
     __syncthreads();
     int maxrows = 0;
 #pragma unroll
@@ -745,6 +759,97 @@ __global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, i
   }
   if (bad) atomicOr(a.flag, 1);
   if (late) atomicOr(a.flag, 2);  // a bounded wait gave up: reported as SHM_ERR_TIMEOUT
+}
+
+// One time step per launch (CUDA-graph chunks of launches advance a plan).
+template <int EW, bool kSensor, bool kAdj = false>
+__global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_step_f32(F32Args a, int kstep) {
+  __shared__ __align__(8) unsigned long long bar_mem;
+  const unsigned bar = smem_u32(&bar_mem);
+  if (threadIdx.x == 0) mbar_init(bar, 1);  // (made visible by the step's first CTA barrier)
+  unsigned phase = 0;
+  struct_f32_step<EW, kSensor, kAdj>(a, kstep, bar, phase);
+}
+
+// --- persistent stepping -----------------------------------------------------
+// Device-wide barrier between the steps of a persistent launch, on one word
+// that the host zeroes before each launch: every CTA adds 1 when it arrives
+// (a releasing add), so barrier k is complete when the count reaches
+// (k + 1) x gridDim.x, which each CTA then reads with acquiring loads.  Bit 31
+// is the abort bit: a CTA whose wait runs out of polls sets it, and every CTA
+// leaves at its next barrier instead of waiting (the host reads
+// SHM_ERR_TIMEOUT from the flag).  The count stays below bit 31 because the
+// host splits runs so that steps x CTAs < 2^30.
+struct GridSync {
+  unsigned* ctr;
+  int spin;  // polls before a wait gives up
+};
+constexpr unsigned kGridAbort = 0x80000000u;
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned atom_add_release_gpu(unsigned* p, unsigned x) {
+  unsigned old;
+  asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(x) : "memory");
+  return old;
+}
+
+// Barrier number k of the launch.  Returns false (in every thread of the
+// CTA) when the CTA must stop.
+__device__ __forceinline__ bool grid_sync(const GridSync& gs, unsigned k, int* flag) {
+  __shared__ int s_go;
+  __syncthreads();  // the CTA's stores of this step before its arrival
+  if (threadIdx.x == 0) {
+    const unsigned target = (k + 1) * gridDim.x;
+    const unsigned old = atom_add_release_gpu(gs.ctr, 1u);
+    int go = 0;
+    if (!(old & kGridAbort)) {
+      if (old + 1 == target) {
+        go = 1;  // the last CTA to arrive
+      } else {
+        for (int it = 0; it < gs.spin; ++it) {
+          const unsigned v = ld_acquire_gpu(gs.ctr);
+          if (v & kGridAbort) break;
+          if (v >= target) {
+            go = 1;
+            break;
+          }
+        }
+        if (!go) {
+          atomicOr(gs.ctr, kGridAbort);
+          atomicOr(flag, 2);
+        }
+      }
+    }
+    s_go = go;
+  }
+  __syncthreads();
+  const bool go = s_go != 0;
+  // the next step's bulk copies (async proxy) read other CTAs' stores of
+  // this step (generic proxy), which the acquire above made visible
+  asm volatile("fence.proxy.async.global;\n" ::: "memory");
+  return go;
+}
+
+// All `nsteps` steps in one cooperative launch: every CTA is resident, and
+// the CTAs meet at a device-wide barrier between steps where consecutive
+// launches would meet at the kernel boundary.  The grid may be smaller than
+// the task list (each CTA takes every gridDim.x-th task group in each step).
+template <int EW, bool kSensor>
+__global__ void __launch_bounds__(CTA_THREADS, 2) k_struct_run_f32(F32Args a, int nsteps, GridSync gs) {
+  __shared__ __align__(8) unsigned long long bar_mem;
+  const unsigned bar = smem_u32(&bar_mem);
+  if (threadIdx.x == 0) mbar_init(bar, 1);
+  unsigned phase = 0;
+  // with at most one task group per CTA, the CTA keeps its group across steps
+  const bool single = (a.ntask + F32Geom<EW>::G - 1) / F32Geom<EW>::G <= (int)gridDim.x;
+  for (int k = 0; k < nsteps; ++k) {
+    struct_f32_step<EW, kSensor, false>(a, k, bar, phase, single && k > 0);
+    if (k + 1 < nsteps && !grid_sync(gs, (unsigned)k, a.flag)) break;
+  }
 }
 
 }  // namespace shm

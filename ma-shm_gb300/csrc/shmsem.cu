@@ -420,6 +420,12 @@ struct shm_plan {
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
   bool ran = false;
+  // persistent stepping (FP32 structured plans): one cooperative launch per
+  // advance, CTAs meeting at a device-wide barrier between steps
+  bool persistent = false;
+  int spin_limit = 1 << 22;    // barrier polls before a wait gives up
+  unsigned* gsync = nullptr;   // barrier word: arrivals, bit 31 = abort
+  int coop_max = 0;            // co-resident CTAs of the persistent kernel
 };
 
 #define CKP(plan, call)                                                               \
@@ -734,6 +740,14 @@ static shm_status set_func_attrs(shm_plan* p) {
   CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_f32_smem_bytes<16>()));
   CKP(p, cudaFuncSetAttribute(k_struct_step_f32<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_run_f32<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_run_f32<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<32>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_run_f32<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)struct_f32_smem_bytes<16>()));
+  CKP(p, cudaFuncSetAttribute(k_struct_run_f32<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_f32_smem_bytes<16>()));
   CKP(p, cudaFuncSetAttribute(k_struct_step_f32<32, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)struct_f32_smem_bytes<32>()));
@@ -1097,6 +1111,30 @@ static F32Args struct_f32_args(shm_plan* p) {
   a.o_q = sp.o_q;
   a.e_of_g = sp.e_of_g;
   return a;
+}
+
+// Persistent FP32 structured stepping: `nsteps` steps in one cooperative
+// launch of at most coop_max CTAs (all resident at once, which the barrier
+// between steps needs; the runtime refuses a larger cooperative grid).
+static cudaError_t launch_struct_run_f32(shm_plan* p, int nsteps, cudaStream_t s) {
+  StructPlan& sp = p->sp;
+  F32Args a = struct_f32_args(p);
+  const bool sens = p->nslot > 0;
+  cudaError_t e = cudaMemsetAsync(p->gsync, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  GridSync gs{p->gsync, p->spin_limit};
+  void* args[] = {&a, &nsteps, &gs};
+  const int grid = std::max(1, std::min(sp.grid, p->coop_max));
+  const void* fn;
+  size_t smem;
+  if (sp.tile == 32) {
+    fn = sens ? (const void*)k_struct_run_f32<32, true> : (const void*)k_struct_run_f32<32, false>;
+    smem = struct_f32_smem_bytes<32>();
+  } else {
+    fn = sens ? (const void*)k_struct_run_f32<16, true> : (const void*)k_struct_run_f32<16, false>;
+    smem = struct_f32_smem_bytes<16>();
+  }
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CTA_THREADS), args, smem, s);
 }
 
 static cudaError_t launch_struct_step_f32(shm_plan* p, int kstep, cudaStream_t s) {
@@ -1695,6 +1733,21 @@ static shm_status advance_async(shm_plan* p, int nsteps, cudaStream_t s) {
   if (p->nn + nsteps > p->nft + 1) return bad(p, "advance past nft");
   shm_status st = ensure_graph(p, s);
   if (st != SHM_OK) return st;
+  if (p->persistent && p->path == 2 && nsteps > 0) {
+    // runs of at most 2^30 / CTAs steps keep the barrier count below its abort bit
+    const int grid = std::max(1, std::min(p->sp.grid, p->coop_max));
+    const int chunk = std::max(1, (1 << 30) / grid);
+    for (int done = 0; done < nsteps;) {
+      const int n = std::min(chunk, nsteps - done);
+      CKP(p, launch_struct_run_f32(p, n, s));
+      k_advance<<<1, 1, 0, s>>>(p->d_base, n);
+      CKP(p, cudaGetLastError());
+      done += n;
+    }
+    p->nn += nsteps;
+    p->ran = true;
+    return SHM_OK;
+  }
   int left = nsteps;
   while (p->gexec && left >= p->gsteps) {
     CKP(p, cudaGraphLaunch(p->gexec, s));
@@ -1715,7 +1768,7 @@ static shm_status check_flag(shm_plan* p, cudaStream_t s) {
   CKP(p, cudaMemcpyAsync(&flag, p->flag, 4, cudaMemcpyDeviceToHost, s));
   CKP(p, cudaStreamSynchronize(s));
   if (flag & 2) {
-    p->err = "a bounded device-side wait gave up (bulk copies did not complete)";
+    p->err = "a bounded device-side wait gave up (bulk copies or the persistent step barrier)";
     return SHM_ERR_TIMEOUT;
   }
   if (flag) {
@@ -1919,7 +1972,7 @@ extern "C" shm_status shm_plan_info(const shm_plan* p, int64_t* info) {
   info[3] = p->path;
   info[4] = p->prec;
   info[5] = p->nframes;
-  info[6] = p->path == 2 ? 1 : 2;
+  info[6] = p->path == 2 ? (p->persistent ? 0 : 1) : 2;  // 0: one launch per advance
   info[7] = p->path == 2 ? p->sp.tile : 0;
   info[8] = p->path == 2 ? p->sp.H : 0;
   info[9] = p->nfields;
@@ -1946,6 +1999,53 @@ extern "C" shm_status shm_set_guard_interval(shm_plan* p, int32_t steps) {
   p->guard_int = steps;
   p->fspec.guard_int = steps;
   drop_graph(p);  // the step kernels' arguments are captured by value
+  return SHM_OK;
+}
+
+// whether the plan can step persistently; sets coop_max and allocates the
+// barrier words on first use
+static shm_status persistent_ready(shm_plan* p) {
+  if (p->kind != 0 || p->prec != 32 || p->sp_generic || p->path != 2)
+    return bad(p, "persistent stepping needs an FP32 plan on the structured fused kernel");
+  if (!p->gsync) {
+    int coop = 0, nsm = 0;
+    CKP(p, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, p->device));
+    if (!coop) {
+      p->err = "the device does not support cooperative launches";
+      return SHM_ERR_UNSUPPORTED;
+    }
+    CKP(p, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+    int per_sm[4] = {0, 0, 0, 0};
+    CKP(p, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_struct_run_f32<32, false>, CTA_THREADS,
+                                                         struct_f32_smem_bytes<32>()));
+    CKP(p, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_struct_run_f32<32, true>, CTA_THREADS,
+                                                         struct_f32_smem_bytes<32>()));
+    CKP(p, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], k_struct_run_f32<16, false>, CTA_THREADS,
+                                                         struct_f32_smem_bytes<16>()));
+    CKP(p, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[3], k_struct_run_f32<16, true>, CTA_THREADS,
+                                                         struct_f32_smem_bytes<16>()));
+    const int m = *std::min_element(per_sm, per_sm + 4);
+    if (m < 1) {
+      p->err = "the persistent kernel does not fit on a multiprocessor";
+      return SHM_ERR_UNSUPPORTED;
+    }
+    unsigned* g = nullptr;
+    shm_status st = dalloc(p, &g, 4);
+    if (st != SHM_OK) return st;
+    p->gsync = g;
+    p->coop_max = m * nsm;
+  }
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_set_persistent(shm_plan* p, int32_t enable, int32_t spin_limit) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (enable) {
+    shm_status st = persistent_ready(p);
+    if (st != SHM_OK) return st;
+  }
+  p->persistent = enable != 0;
+  p->spin_limit = spin_limit < 0 ? (1 << 22) : spin_limit;
   return SHM_OK;
 }
 
@@ -1983,6 +2083,12 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
   }
   float best = 1e30f;
   int bt = p->sp.tile, bh = p->sp.H;
+  bool bp = false;
+  // every structured candidate is also timed as a persistent launch when the
+  // plan and the device allow it
+  const bool can_persist = persistent_ready(p) == SHM_OK;
+  if (!can_persist) p->err.clear();
+  p->persistent = false;
   // candidate 0: the general element + node kernels
   {
     p->path = 1;
@@ -2000,17 +2106,22 @@ extern "C" shm_status shm_autotune(shm_plan* p, int32_t steps, int32_t* tile_out
     for (int H : cand[ti]) {
       shm_status st = struct_tasks(p, tiles[ti], H);
       if (st != SHM_OK) return st;
-      drop_graph(p);
-      if ((st = shm_reset(p)) != SHM_OK) return st;
-      if ((st = advance_async(p, warm, p->stream)) != SHM_OK) return st;
-      float ms = 0.f;
-      if ((st = shm_time_steps(p, steps, &ms)) != SHM_OK) return st;
-      if (ms < best) {
-        best = ms;
-        bt = tiles[ti];
-        bh = H;
+      for (int pers = 0; pers <= (can_persist ? 1 : 0); ++pers) {
+        p->persistent = pers != 0;
+        drop_graph(p);
+        if ((st = shm_reset(p)) != SHM_OK) return st;
+        if ((st = advance_async(p, warm, p->stream)) != SHM_OK) return st;
+        float ms = 0.f;
+        if ((st = shm_time_steps(p, steps, &ms)) != SHM_OK) return st;
+        if (ms < best) {
+          best = ms;
+          bt = tiles[ti];
+          bh = H;
+          bp = pers != 0;
+        }
       }
     }
+  p->persistent = bt != 0 && bp;
   shm_status st = SHM_OK;
   if (bt == 0) {
     p->path = 1;  // the general kernels were fastest

@@ -88,14 +88,16 @@ class Plan:
         self.lib.shm_plan_info(self.handle, info)
         self.info = dict(nnode=info[0], fen=info[1], ndof=info[2], path=info[3], precision=info[4],
                          nframes=info[5], launches_per_step=info[6], tile=info[7], rows_per_block=info[8],
-                         nfields=info[9])
+                         nfields=info[9], persistent=info[3] == 2 and info[6] == 0)
 
     def autotune(self, steps: int = 20):
-        """Pick the structured kernel's lane-group width and rows per task by timing."""
+        """Pick the structured kernel's lane-group width, rows per task and
+        launch mode (per-step launches or one persistent launch) by timing."""
         t, r, ms = C.c_int32(), C.c_int32(), C.c_float()
         self._check(self.lib.shm_autotune(self.handle, int(steps), C.byref(t), C.byref(r), C.byref(ms)))
         self._refresh_info()
-        return dict(tile=t.value, rows_per_block=r.value, ms_per_step=ms.value)
+        return dict(tile=t.value, rows_per_block=r.value, persistent=self.info["persistent"],
+                    ms_per_step=ms.value)
 
     def forward_backward(self, target, signals=None, ckpt_every: int = 200):
         """Misfit J (per scenario) and dJ/dd_e (d_e = 1 - elem_keep) by the
@@ -113,6 +115,14 @@ class Plan:
             out.append(grad[e0:e0 + fen].copy())
             e0 += fen
         return mis, out
+
+    def set_persistent(self, enable: bool = True, spin_limit: int = -1):
+        """Advance in one cooperative launch per call, the CTAs meeting at a
+        device-wide barrier between steps (FP32 plans on the structured fused
+        kernel).  ``spin_limit`` bounds each barrier wait in polls (< 0: the
+        default); a wait that runs out raises SHM_ERR_TIMEOUT."""
+        self._check(self.lib.shm_set_persistent(self.handle, int(bool(enable)), int(spin_limit)))
+        self._refresh_info()
 
     def set_guard_interval(self, steps: int):
         """Blow-up guard every ``steps`` time steps besides the frame steps

@@ -229,8 +229,9 @@ def test_autotune_picks_a_config_and_keeps_results(pkg):
     plan = pkg.Plan(scs, run, precision=32, path=2, steps_per_graph=20)
     best = plan.autotune(5)
     assert best["tile"] in (0, 16, 32) and 1 <= best["rows_per_block"] <= 64
+    assert best["persistent"] in (False, True) and best["persistent"] == plan.info["persistent"]
     if best["tile"] == 0:
-        assert plan.info["path"] == 1
+        assert plan.info["path"] == 1 and not best["persistent"]
     else:
         assert plan.info["tile"] == best["tile"] and plan.info["rows_per_block"] == best["rows_per_block"]
     tuned = plan.forward()
