@@ -426,6 +426,10 @@ struct shm_plan {
   int spin_limit = 1 << 22;    // barrier polls before a wait gives up
   unsigned* gsync = nullptr;   // barrier word: arrivals, bit 31 = abort
   int coop_max = 0;            // co-resident CTAs of the persistent kernel
+  // frames to the caller: two device and two pinned staging buffers
+  double* fstage = nullptr;
+  double* hstage = nullptr;
+  cudaEvent_t fev[2] = {nullptr, nullptr};
 };
 
 #define CKP(plan, call)                                                               \
@@ -1661,6 +1665,9 @@ extern "C" shm_status shm_plan_destroy(shm_plan* p) {
   if (!p) return SHM_OK;
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   for (void* q : p->allocs) cudaFree(q);
+  if (p->hstage) cudaFreeHost(p->hstage);
+  for (cudaEvent_t e : p->fev)
+    if (e) cudaEventDestroy(e);
   if (p->stream) cudaStreamDestroy(p->stream);
   for (cudaStream_t a : p->aux)
     if (a) cudaStreamDestroy(a);
@@ -1809,19 +1816,90 @@ extern "C" shm_status shm_time_steps(shm_plan* p, int32_t nsteps, float* ms) {
   return check_flag(p, s);
 }
 
+// One piece of the frames: rows r = 0 .. nr-1 of `src` (row stride `row`),
+// columns 0 .. nc-1, packed ([r][nc]) and widened to FP64
 template <typename T>
-static void to_host_frames(const std::vector<T>& dev, shm_plan* p, double* frames) {
-  // device [nframes][nfields][nnode_pad] over all scenarios
-  //   -> [nscen][nframes][nfields][nnode_s]
-  double* o = frames;
-  for (int s = 0; s < p->nscen; ++s) {
-    const int64_t n0 = p->node_off[s], nn = p->node_off[s + 1] - n0;
-    for (int c = 0; c < p->nframes; ++c)
-      for (int f = 0; f < p->nfields; ++f) {
-        const T* src = dev.data() + ((size_t)c * p->nfields + f) * p->nnode_pad + n0;
-        for (int64_t g = 0; g < nn; ++g) *o++ = (double)src[g];
-      }
+__global__ void k_pack_frames(const T* __restrict__ src, double* __restrict__ dst, int64_t row, int64_t nc,
+                              int64_t nr) {
+  const int64_t n = nr * nc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / nc;
+    dst[i] = (double)src[r * row + (i - r * nc)];
   }
+}
+
+// Frames to the caller: device [nframes][nfields][nnode_pad] over all
+// scenarios (row = frame x nfields + field) -> host
+// [nscen][nframes][nfields][nnode_s] in FP64.  The host array is cut into
+// contiguous pieces of at most 4 M values: runs of whole rows of one
+// scenario's node range, or parts of one row when a row alone is larger.
+// Each piece is packed and widened on the device into one of two staging
+// buffers, moved to pinned host memory by the copy engine, and copied into
+// the caller's array by the host while the next piece is in flight
+// (pageable destinations never see a DMA).
+static shm_status frames_to_host(shm_plan* p, double* frames, cudaStream_t s) {
+  constexpr int64_t kStage = (int64_t)4 << 20;  // doubles per staging buffer (32 MB)
+  const int64_t row = p->nnode_pad;
+  const int64_t rows = (int64_t)p->nframes * p->nfields;
+  if (!p->fstage) {
+    double* b = nullptr;
+    shm_status st = dalloc(p, &b, 2 * (size_t)kStage);
+    if (st != SHM_OK) return st;
+    p->fstage = b;
+  }
+  if (!p->hstage) {
+    void* h = nullptr;
+    CKP(p, cudaMallocHost(&h, 2 * kStage * sizeof(double)));
+    p->hstage = static_cast<double*>(h);
+  }
+  for (int k = 0; k < 2; ++k)
+    if (!p->fev[k]) CKP(p, cudaEventCreateWithFlags(&p->fev[k], cudaEventDisableTiming));
+  double* pend_dst[2] = {nullptr, nullptr};
+  int64_t pend_n[2] = {0, 0};
+  auto flush = [&](int b) -> shm_status {
+    if (pend_dst[b]) {
+      CKP(p, cudaEventSynchronize(p->fev[b]));
+      std::memcpy(pend_dst[b], p->hstage + b * kStage, pend_n[b] * sizeof(double));
+      pend_dst[b] = nullptr;
+    }
+    return SHM_OK;
+  };
+  int b = 0;
+  int64_t host_off = 0;
+  for (int sc = 0; sc < p->nscen; ++sc) {
+    const int64_t n0 = p->node_off[sc], nn = p->node_off[sc + 1] - n0;
+    const int64_t cw = std::min(nn, kStage);                       // columns per piece
+    const int64_t per = nn <= kStage ? std::max<int64_t>(1, kStage / std::max<int64_t>(nn, 1)) : 1;
+    for (int64_t r0 = 0; r0 < rows; r0 += per) {
+      const int64_t nr = std::min(per, rows - r0);
+      for (int64_t c0 = 0; c0 < nn; c0 += cw) {
+        const int64_t nc = std::min(cw, nn - c0);
+        const int64_t n = nr * nc;
+        shm_status st = flush(b);  // buffer b is free once its previous piece is out
+        if (st != SHM_OK) return st;
+        const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+        const int64_t so = r0 * row + n0 + c0;
+        if (p->prec == 32)
+          k_pack_frames<float><<<blocks, 256, 0, s>>>((const float*)p->frames + so, p->fstage + b * kStage, row, nc, nr);
+        else
+          k_pack_frames<double><<<blocks, 256, 0, s>>>((const double*)p->frames + so, p->fstage + b * kStage, row, nc,
+                                                       nr);
+        CKP(p, cudaGetLastError());
+        CKP(p, cudaMemcpyAsync(p->hstage + b * kStage, p->fstage + b * kStage, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+        CKP(p, cudaEventRecord(p->fev[b], s));
+        pend_dst[b] = frames + host_off + r0 * nn + c0;  // nr == 1 whenever nc < nn
+        pend_n[b] = n;
+        b ^= 1;
+      }
+    }
+    host_off += rows * nn;
+  }
+  for (int k = 0; k < 2; ++k, b ^= 1) {
+    shm_status st = flush(b);
+    if (st != SHM_OK) return st;
+  }
+  return SHM_OK;
 }
 
 extern "C" shm_status shm_read_outputs(shm_plan* p, double* displ, double* voltage, double* frames,
@@ -1837,18 +1915,8 @@ extern "C" shm_status shm_read_outputs(shm_plan* p, double* displ, double* volta
     CKP(p, cudaMemcpyAsync(voltage, p->volt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   }
   if (frames && p->nframes > 0) {
-    const size_t cnt = (size_t)p->nframes * p->nfields * p->nnode_pad;
-    if (p->prec == 64) {
-      std::vector<double> h(cnt);
-      CKP(p, cudaMemcpyAsync(h.data(), p->frames, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
-      CKP(p, cudaStreamSynchronize(s));
-      to_host_frames(h, p, frames);
-    } else {
-      std::vector<float> h(cnt);
-      CKP(p, cudaMemcpyAsync(h.data(), p->frames, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s));
-      CKP(p, cudaStreamSynchronize(s));
-      to_host_frames(h, p, frames);
-    }
+    shm_status st = frames_to_host(p, frames, s);
+    if (st != SHM_OK) return st;
   }
   CKP(p, cudaStreamSynchronize(s));
   return SHM_OK;

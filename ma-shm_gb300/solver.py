@@ -249,7 +249,8 @@ class Plan:
             res = dict(displ=d, voltage=v)
             if frames is not None:
                 nfr, nfl = self.info["nframes"], self.info["nfields"]
-                res["frames"] = frames[fo:fo + nfr * nfl * nnode].reshape(nfr, nfl, nnode).copy()
+                # a view: the scenarios' frames are disjoint slices of one array
+                res["frames"] = frames[fo:fo + nfr * nfl * nnode].reshape(nfr, nfl, nnode)
                 fo += nfr * nfl * nnode
             out.append(res)
             o += no
