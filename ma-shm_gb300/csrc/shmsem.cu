@@ -2568,10 +2568,18 @@ static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.flag = p->flag;
   a.d_base = p->d_base;
   a.gbox = (const T*)p->gbox;
-  if (p->gbox)
-    k_elem_solid<T, true><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
-  else
-    k_elem_solid<T, false><<<(int)(p->fen_pad / S_EPB), S_THREADS, 0, s>>>(a, kstep);
+  if constexpr (sizeof(T) == 4) {  // node lines
+    using SL = SolidLines<T>;
+    if (p->gbox)
+      k_elem_solid<T, true><<<(int)(p->fen_pad / SL::EPB), SL::THREADS, SL::SMEM, s>>>(a, kstep);
+    else
+      k_elem_solid<T, false><<<(int)(p->fen_pad / SL::EPB), SL::THREADS, SL::SMEM, s>>>(a, kstep);
+  } else {  // a thread per node
+    if (p->gbox)
+      k_elem_solid_nodes<T, true><<<(int)(p->fen_pad / S_NODE_EPB), S_NODE_THREADS, 0, s>>>(a, kstep);
+    else
+      k_elem_solid_nodes<T, false><<<(int)(p->fen_pad / S_NODE_EPB), S_NODE_THREADS, 0, s>>>(a, kstep);
+  }
   k_node_solid<T><<<(int)((p->nnode + 255) / 256), 256, 0, s>>>(a, kstep);
   return cudaGetLastError();
 }
@@ -2589,6 +2597,12 @@ static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const 
   shm_status s;
   T *g = nullptr, *k = nullptr, *m = nullptr, *mi = nullptr, *ua = nullptr, *ub = nullptr, *f2 = nullptr,
     *fr = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    CKP(p, cudaFuncSetAttribute(k_elem_solid<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SolidLines<T>::SMEM));
+    CKP(p, cudaFuncSetAttribute(k_elem_solid<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SolidLines<T>::SMEM));
+  }
   if ((s = upload(p, &p->conn, conn)) != SHM_OK) return s;
   if (gbox) {  // box elements: the per-node geometry is not needed on the device
     T* gb = nullptr;
