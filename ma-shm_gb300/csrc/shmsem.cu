@@ -426,6 +426,7 @@ struct shm_plan {
   int spin_limit = 1 << 22;    // barrier polls before a wait gives up
   unsigned* gsync = nullptr;   // barrier word: arrivals, bit 31 = abort
   int coop_max = 0;            // co-resident CTAs of the persistent kernel
+  int solid_grid = 0;          // FP32 3D solid: CTAs of the element kernel (resident at once)
   // frames to the caller: two device and two pinned staging buffers
   double* fstage = nullptr;
   double* hstage = nullptr;
@@ -2568,12 +2569,14 @@ static cudaError_t launch_solid_step(shm_plan* p, int kstep, cudaStream_t s) {
   a.flag = p->flag;
   a.d_base = p->d_base;
   a.gbox = (const T*)p->gbox;
-  if constexpr (sizeof(T) == 4) {  // node lines
+  if constexpr (sizeof(T) == 4) {  // node lines, on the resident grid
     using SL = SolidLines<T>;
+    const int groups = (int)(p->fen_pad / SL::EPB);
+    const int grid = p->solid_grid > 0 ? std::min(groups, p->solid_grid) : groups;
     if (p->gbox)
-      k_elem_solid<T, true><<<(int)(p->fen_pad / SL::EPB), SL::THREADS, SL::SMEM, s>>>(a, kstep);
+      k_elem_solid<T, true><<<grid, SL::THREADS, SL::SMEM, s>>>(a, kstep);
     else
-      k_elem_solid<T, false><<<(int)(p->fen_pad / SL::EPB), SL::THREADS, SL::SMEM, s>>>(a, kstep);
+      k_elem_solid<T, false><<<grid, SL::THREADS, SL::SMEM, s>>>(a, kstep);
   } else {  // a thread per node
     if (p->gbox)
       k_elem_solid_nodes<T, true><<<(int)(p->fen_pad / S_NODE_EPB), S_NODE_THREADS, 0, s>>>(a, kstep);
@@ -2602,6 +2605,12 @@ static shm_status solid_device(shm_plan* p, const std::vector<int>& conn, const 
                                 (int)SolidLines<T>::SMEM));
     CKP(p, cudaFuncSetAttribute(k_elem_solid<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)SolidLines<T>::SMEM));
+    // the element kernel loops over element groups on the CTAs that fit at once
+    int nsm = 0, per_sm = 0;
+    CKP(p, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+    CKP(p, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_elem_solid<T, false>, SolidLines<T>::THREADS,
+                                                         SolidLines<T>::SMEM));
+    p->solid_grid = std::max(1, per_sm) * nsm;
   }
   if ((s = upload(p, &p->conn, conn)) != SHM_OK) return s;
   if (gbox) {  // box elements: the per-node geometry is not needed on the device

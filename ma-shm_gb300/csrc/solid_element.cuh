@@ -127,7 +127,6 @@ __global__ void __launch_bounds__(SolidLines<T>::THREADS) k_elem_solid(SolidArgs
   }
   const int le = threadIdx.x / S_TPE;
   const int t = threadIdx.x % S_TPE;
-  const int e = blockIdx.x * EPB + le;
   T* const base = reinterpret_cast<T*>(s_raw) + le * S_ES;
   T* const su = base;                 // [3][108] node order, later the xi-line forces
   T* const suT = base + 3 * S_NPE;    // [3][108] eta-major, later the eta-line forces
@@ -143,86 +142,50 @@ __global__ void __launch_bounds__(SolidLines<T>::THREADS) k_elem_solid(SolidArgs
     cTh[h] = cxh[h] * NP + cyh[h];
   }
 
-  // phase 0: gather
+  // The CTA takes element groups blockIdx.x, + gridDim.x, ... (the grid is
+  // what stays resident), and gathers the next group's nodal values into
+  // registers while it computes the current one: the connectivity two groups
+  // ahead, the displacements one group ahead.
+  const int ngroups = (int)(a.fen_pad / EPB);
+  const int G = gridDim.x;
+  int nd[NP];      // node numbers of the next group to gather
+  T uv[NP][3];     // gathered displacements of the group to stage next
+  auto load_conn = [&](int grp) {
 #pragma unroll
-  for (int j = 0; j < NP; ++j) {
-    const int c = t + S_TPE * j;
-    const int node = a.conn[(int64_t)e * S_NPE + c];
-    const int cT = 36 * (j / 2) + cTh[j % 2];
+    for (int j = 0; j < NP; ++j) nd[j] = a.conn[((int64_t)grp * EPB + le) * S_NPE + t + S_TPE * j];
+  };
+  auto load_u = [&]() {
 #pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      const T v = cur[f * a.nnode_pad + node];
-      su[f * S_NPE + c] = v;
-      suT[f * S_NPE + cT] = v;
-    }
+    for (int j = 0; j < NP; ++j)
+#pragma unroll
+      for (int f = 0; f < 3; ++f) uv[j][f] = cur[f * a.nnode_pad + nd[j]];
+  };
+  if (blockIdx.x < ngroups) {
+    load_conn(blockIdx.x);
+    load_u();
+    if (blockIdx.x + G < ngroups) load_conn(blockIdx.x + G);
   }
-  __syncthreads();
-
-  const int lo = (t / NP) * 36 + (t % NP) * NP;  // first value of the thread's xi line (node order)
-                                                 // and of its eta line (eta-major order)
-  auto ld6 = [](const T* p, T (&o)[NP]) {
+  for (int grp = blockIdx.x; grp < ngroups; grp += G) {
+    const int e = grp * EPB + le;
+    __syncthreads();  // the previous group is done with the shared buffers
+    // phase 0: stage the gathered values in both orders, start the next gathers
 #pragma unroll
-    for (int k = 0; k < NP / 2; ++k) {
-      const T2 v = reinterpret_cast<const T2*>(p)[k];
-      o[2 * k] = v.x;
-      o[2 * k + 1] = v.y;
-    }
-  };
-  auto st6 = [](T* p, const T (&o)[NP]) {
+    for (int j = 0; j < NP; ++j) {
+      const int c = t + S_TPE * j;
+      const int cT = 36 * (j / 2) + cTh[j % 2];
 #pragma unroll
-    for (int k = 0; k < NP / 2; ++k) {
-      T2 v;
-      v.x = o[2 * k];
-      v.y = o[2 * k + 1];
-      reinterpret_cast<T2*>(p)[k] = v;
-    }
-  };
-  // phase 1: reference derivatives (Npx*U, Npy*U, Npz*U) along lines
-#pragma unroll
-  for (int f = 0; f < 3; ++f) {
-    T u[NP], d[NP];
-    ld6(su + f * S_NPE + lo, u);
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      T s = T(0);
-#pragma unroll
-      for (int m = 0; m < NP; ++m) s = fma(Dm<T>(i, m), u[m], s);
-      d[i] = s;
-    }
-    st6(sd + (f * 3 + 0) * S_NPE + lo, d);
-    ld6(suT + f * S_NPE + lo, u);
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      T s = T(0);
-#pragma unroll
-      for (int m = 0; m < NP; ++m) s = fma(Dm<T>(i, m), u[m], s);
-      d[i] = s;
-    }
-    st6(sd + (f * 3 + 1) * S_NPE + lo, d);
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int q = t + S_TPE * h;
-      T z[S_NZ];
-#pragma unroll
-      for (int m = 0; m < S_NZ; ++m) z[m] = su[f * S_NPE + m * 36 + q];
-#pragma unroll
-      for (int i = 0; i < S_NZ; ++i) {
-        T s = T(0);
-#pragma unroll
-        for (int m = 0; m < S_NZ; ++m) s = fma(D3m<T>(i, m), z[m], s);
-        sd[(f * 3 + 2) * S_NPE + i * 36 + q] = s;
+      for (int f = 0; f < 3; ++f) {
+        su[f * S_NPE + c] = uv[j][f];
+        suT[f * S_NPE + cT] = uv[j][f];
       }
     }
-  }
-  __syncthreads();
-
-  // phase 2: per node, strains_spec_p.m / stresses_spec_p.m and the fluxes
-  {
-    const T* __restrict__ Dm_ = a.mat + (int64_t)a.emat[e] * S_MAT_DEV;
+    if (grp + G < ngroups) {
+      load_u();
+      if (grp + 2 * G < ngroups) load_conn(grp + 2 * G);
+    }
+    // this group's per-element numbers for phase 2, ahead of phase 1
+    const int mat_e = a.emat[e];
     const T kp = a.ekeep[e];
-    const T D11 = Dm_[0] * kp, D12 = Dm_[1] * kp, D13 = Dm_[2] * kp, D14 = Dm_[3] * kp, D22 = Dm_[4] * kp;
-    const T D23 = Dm_[5] * kp, D24 = Dm_[6] * kp, D33 = Dm_[7] * kp, D34 = Dm_[8] * kp, D44 = Dm_[9] * kp;
-    const T D55 = Dm_[10] * kp, D56 = Dm_[11] * kp, D66 = Dm_[12] * kp;
     T bx = T(0), by = T(0), bz = T(0), bv = T(0);
     if constexpr (kBox) {
       bx = a.gbox[e];
@@ -230,94 +193,161 @@ __global__ void __launch_bounds__(SolidLines<T>::THREADS) k_elem_solid(SolidArgs
       bz = a.gbox[2 * a.fen_pad + e];
       bv = a.gbox[3 * a.fen_pad + e];
     }
+    __syncthreads();
+
+    const int lo = (t / NP) * 36 + (t % NP) * NP;  // first value of the thread's xi line (node order)
+                                                   // and of its eta line (eta-major order)
+    auto ld6 = [](const T* p, T (&o)[NP]) {
+#pragma unroll
+      for (int k = 0; k < NP / 2; ++k) {
+        const T2 v = reinterpret_cast<const T2*>(p)[k];
+        o[2 * k] = v.x;
+        o[2 * k + 1] = v.y;
+      }
+    };
+    auto st6 = [](T* p, const T (&o)[NP]) {
+#pragma unroll
+      for (int k = 0; k < NP / 2; ++k) {
+        T2 v;
+        v.x = o[2 * k];
+        v.y = o[2 * k + 1];
+        reinterpret_cast<T2*>(p)[k] = v;
+      }
+    };
+    // phase 1: reference derivatives (Npx*U, Npy*U, Npz*U) along lines
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      T u[NP], d[NP];
+      ld6(su + f * S_NPE + lo, u);
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int m = 0; m < NP; ++m) s = fma(Dm<T>(i, m), u[m], s);
+        d[i] = s;
+      }
+      st6(sd + (f * 3 + 0) * S_NPE + lo, d);
+      ld6(suT + f * S_NPE + lo, u);
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int m = 0; m < NP; ++m) s = fma(Dm<T>(i, m), u[m], s);
+        d[i] = s;
+      }
+      st6(sd + (f * 3 + 1) * S_NPE + lo, d);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = t + S_TPE * h;
+        T z[S_NZ];
+#pragma unroll
+        for (int m = 0; m < S_NZ; ++m) z[m] = su[f * S_NPE + m * 36 + q];
+#pragma unroll
+        for (int i = 0; i < S_NZ; ++i) {
+          T s = T(0);
+#pragma unroll
+          for (int m = 0; m < S_NZ; ++m) s = fma(D3m<T>(i, m), z[m], s);
+          sd[(f * 3 + 2) * S_NPE + i * 36 + q] = s;
+        }
+      }
+    }
+    __syncthreads();
+
+    // phase 2: per node, strains_spec_p.m / stresses_spec_p.m and the fluxes
+    {
+      const T* __restrict__ Dm_ = a.mat + (int64_t)mat_e * S_MAT_DEV;
+      const T D11 = Dm_[0] * kp, D12 = Dm_[1] * kp, D13 = Dm_[2] * kp, D14 = Dm_[3] * kp, D22 = Dm_[4] * kp;
+      const T D23 = Dm_[5] * kp, D24 = Dm_[6] * kp, D33 = Dm_[7] * kp, D34 = Dm_[8] * kp, D44 = Dm_[9] * kp;
+      const T D55 = Dm_[10] * kp, D56 = Dm_[11] * kp, D66 = Dm_[12] * kp;
 #pragma unroll 2
+      for (int j = 0; j < NP; ++j) {
+        const int c = t + S_TPE * j;
+        const int cT = 36 * (j / 2) + cTh[j % 2];
+        const int cx = cxh[j % 2], cy = cyh[j % 2], cz = j / 2;
+        T iJ[3][3];
+        T W;
+        if constexpr (kBox) {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = T(0);
+          iJ[0][0] = bx;
+          iJ[1][1] = by;
+          iJ[2][2] = bz;
+          W = sW[cx] * sW[cy] * sW3[cz] * bv;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * a.fen_pad + e) * S_NPE + c];
+          W = a.geo[((int64_t)9 * a.fen_pad + e) * S_NPE + c];
+        }
+        T g[3][3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const T d0 = sd[(f * 3 + 0) * S_NPE + c], d1 = sd[(f * 3 + 1) * S_NPE + cT], d2 = sd[(f * 3 + 2) * S_NPE + c];
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            g[f][b] = kBox ? (b == 0 ? d0 : b == 1 ? d1 : d2) * iJ[b][b] : d0 * iJ[0][b] + d1 * iJ[1][b] + d2 * iJ[2][b];
+        }
+        const T Exx = g[0][0], Eyy = g[1][1], Ezz = g[2][2];
+        const T Exy = g[0][1] + g[1][0];
+        const T Eyz = g[1][2] + g[2][1];
+        const T Exz = g[0][2] + g[2][0];
+        const T Sxx = Exx * D11 + Eyy * D12 + Ezz * D13 + Exy * D14;
+        const T Syy = Exx * D12 + Eyy * D22 + Ezz * D23 + Exy * D24;
+        const T Szz = Exx * D13 + Eyy * D23 + Ezz * D33 + Exy * D34;
+        const T Sxy = Exx * D14 + Eyy * D24 + Ezz * D34 + Exy * D44;
+        const T Syz = Eyz * D55 + Exz * D56;
+        const T Sxz = Eyz * D56 + Exz * D66;
+        // fluxes: field u uses (Sxx, Sxy, Sxz), v (Sxy, Syy, Syz), w (Sxz, Syz, Szz)
+        const T S[3][3] = {{Sxx, Sxy, Sxz}, {Sxy, Syy, Syz}, {Sxz, Syz, Szz}};
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+          for (int aa = 0; aa < 3; ++aa)
+            sd[(f * 3 + aa) * S_NPE + (aa == 1 ? cT : c)] =
+                kBox ? W * (S[f][aa] * iJ[aa][aa]) : W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
+      }
+    }
+    __syncthreads();
+
+    // phase 3: transposed operators Npx' and Npy' along the thread's lines
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      T gl[NP], o[NP];
+      ld6(sd + (f * 3 + 0) * S_NPE + lo, gl);
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int m = 0; m < NP; ++m) s = fma(Dm<T>(m, i), gl[m], s);
+        o[i] = s;
+      }
+      st6(su + f * S_NPE + lo, o);
+      ld6(sd + (f * 3 + 1) * S_NPE + lo, gl);
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int m = 0; m < NP; ++m) s = fma(Dm<T>(m, i), gl[m], s);
+        o[i] = s;
+      }
+      st6(suT + f * S_NPE + lo, o);
+    }
+    __syncthreads();
+
+    // phase 4: per node, + Npz' and out to the element-local force slots
+#pragma unroll
     for (int j = 0; j < NP; ++j) {
       const int c = t + S_TPE * j;
       const int cT = 36 * (j / 2) + cTh[j % 2];
-      const int cx = cxh[j % 2], cy = cyh[j % 2], cz = j / 2;
-      T iJ[3][3];
-      T W;
-      if constexpr (kBox) {
-#pragma unroll
-        for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = T(0);
-        iJ[0][0] = bx;
-        iJ[1][1] = by;
-        iJ[2][2] = bz;
-        W = sW[cx] * sW[cy] * sW3[cz] * bv;
-      } else {
-#pragma unroll
-        for (int q = 0; q < 9; ++q) iJ[q / 3][q % 3] = a.geo[((int64_t)q * a.fen_pad + e) * S_NPE + c];
-        W = a.geo[((int64_t)9 * a.fen_pad + e) * S_NPE + c];
-      }
-      T g[3][3];
+      const int cz = j / 2, q = t + S_TPE * (j % 2);
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
-        const T d0 = sd[(f * 3 + 0) * S_NPE + c], d1 = sd[(f * 3 + 1) * S_NPE + cT], d2 = sd[(f * 3 + 2) * S_NPE + c];
+        T s = su[f * S_NPE + c] + suT[f * S_NPE + cT];
 #pragma unroll
-        for (int b = 0; b < 3; ++b)
-          g[f][b] = kBox ? (b == 0 ? d0 : b == 1 ? d1 : d2) * iJ[b][b] : d0 * iJ[0][b] + d1 * iJ[1][b] + d2 * iJ[2][b];
+        for (int m = 0; m < S_NZ; ++m) s = fma(sD3[m * S_NZ + cz], sd[(f * 3 + 2) * S_NPE + m * 36 + q], s);
+        a.F2[f * a.plane + (int64_t)e * S_NPE + c] = s;
       }
-      const T Exx = g[0][0], Eyy = g[1][1], Ezz = g[2][2];
-      const T Exy = g[0][1] + g[1][0];
-      const T Eyz = g[1][2] + g[2][1];
-      const T Exz = g[0][2] + g[2][0];
-      const T Sxx = Exx * D11 + Eyy * D12 + Ezz * D13 + Exy * D14;
-      const T Syy = Exx * D12 + Eyy * D22 + Ezz * D23 + Exy * D24;
-      const T Szz = Exx * D13 + Eyy * D23 + Ezz * D33 + Exy * D34;
-      const T Sxy = Exx * D14 + Eyy * D24 + Ezz * D34 + Exy * D44;
-      const T Syz = Eyz * D55 + Exz * D56;
-      const T Sxz = Eyz * D56 + Exz * D66;
-      // fluxes: field u uses (Sxx, Sxy, Sxz), v (Sxy, Syy, Syz), w (Sxz, Syz, Szz)
-      const T S[3][3] = {{Sxx, Sxy, Sxz}, {Sxy, Syy, Syz}, {Sxz, Syz, Szz}};
-#pragma unroll
-      for (int f = 0; f < 3; ++f)
-#pragma unroll
-        for (int aa = 0; aa < 3; ++aa)
-          sd[(f * 3 + aa) * S_NPE + (aa == 1 ? cT : c)] =
-              kBox ? W * (S[f][aa] * iJ[aa][aa]) : W * (S[f][0] * iJ[aa][0] + S[f][1] * iJ[aa][1] + S[f][2] * iJ[aa][2]);
     }
-  }
-  __syncthreads();
-
-  // phase 3: transposed operators Npx' and Npy' along the thread's lines
-#pragma unroll
-  for (int f = 0; f < 3; ++f) {
-    T gl[NP], o[NP];
-    ld6(sd + (f * 3 + 0) * S_NPE + lo, gl);
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      T s = T(0);
-#pragma unroll
-      for (int m = 0; m < NP; ++m) s = fma(Dm<T>(m, i), gl[m], s);
-      o[i] = s;
-    }
-    st6(su + f * S_NPE + lo, o);
-    ld6(sd + (f * 3 + 1) * S_NPE + lo, gl);
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      T s = T(0);
-#pragma unroll
-      for (int m = 0; m < NP; ++m) s = fma(Dm<T>(m, i), gl[m], s);
-      o[i] = s;
-    }
-    st6(suT + f * S_NPE + lo, o);
-  }
-  __syncthreads();
-
-  // phase 4: per node, + Npz' and out to the element-local force slots
-#pragma unroll
-  for (int j = 0; j < NP; ++j) {
-    const int c = t + S_TPE * j;
-    const int cT = 36 * (j / 2) + cTh[j % 2];
-    const int cz = j / 2, q = t + S_TPE * (j % 2);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      T s = su[f * S_NPE + c] + suT[f * S_NPE + cT];
-#pragma unroll
-      for (int m = 0; m < S_NZ; ++m) s = fma(sD3[m * S_NZ + cz], sd[(f * 3 + 2) * S_NPE + m * 36 + q], s);
-      a.F2[f * a.plane + (int64_t)e * S_NPE + c] = s;
-    }
-  }
+  }  // element groups
 }
 
 // Element step with a thread per element node (the FP64 path: the line
