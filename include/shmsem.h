@@ -136,6 +136,14 @@ shm_status shm_forward(shm_plan *plan, const double *st, double *displ, double *
  * shm_advance / shm_forward return SHM_ERR_DIVERGED. */
 shm_status shm_set_guard_interval(shm_plan *plan, int32_t steps);
 
+/* Frames are handed to the caller through two device and two pinned host
+ * staging buffers of `values` FP64 values each (default 4 M = 32 MB each):
+ * runs of frame rows (or parts of a row longer than a buffer) are packed and
+ * widened on the device, copied to pinned memory and from there into the
+ * caller's array while the next run is in flight.  Smaller buffers save
+ * memory at the cost of more copies. */
+shm_status shm_set_frame_staging(shm_plan *plan, int64_t values);
+
 /* Fine-grained stepping used by forward/adjoint drivers and benchmarks. */
 shm_status shm_reset(shm_plan *plan);                        /* zero state, nn = nn_first */
 shm_status shm_set_signal(shm_plan *plan, const double *st, void *stream);

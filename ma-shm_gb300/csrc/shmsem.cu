@@ -427,7 +427,9 @@ struct shm_plan {
   unsigned* gsync = nullptr;   // barrier word: arrivals, bit 31 = abort
   int coop_max = 0;            // co-resident CTAs of the persistent kernel
   int solid_grid = 0;          // FP32 3D solid: CTAs of the element kernel (resident at once)
-  // frames to the caller: two device and two pinned staging buffers
+  // frames to the caller: two device and two pinned staging buffers of
+  // fstage_n values each
+  int64_t fstage_n = (int64_t)4 << 20;
   double* fstage = nullptr;
   double* hstage = nullptr;
   cudaEvent_t fev[2] = {nullptr, nullptr};
@@ -1832,14 +1834,14 @@ __global__ void k_pack_frames(const T* __restrict__ src, double* __restrict__ ds
 // Frames to the caller: device [nframes][nfields][nnode_pad] over all
 // scenarios (row = frame x nfields + field) -> host
 // [nscen][nframes][nfields][nnode_s] in FP64.  The host array is cut into
-// contiguous pieces of at most 4 M values: runs of whole rows of one
+// contiguous pieces of at most fstage_n values (default 4 M, 32 MB): runs of whole rows of one
 // scenario's node range, or parts of one row when a row alone is larger.
 // Each piece is packed and widened on the device into one of two staging
 // buffers, moved to pinned host memory by the copy engine, and copied into
 // the caller's array by the host while the next piece is in flight
 // (pageable destinations never see a DMA).
 static shm_status frames_to_host(shm_plan* p, double* frames, cudaStream_t s) {
-  constexpr int64_t kStage = (int64_t)4 << 20;  // doubles per staging buffer (32 MB)
+  const int64_t kStage = p->fstage_n;  // values per staging buffer
   const int64_t row = p->nnode_pad;
   const int64_t rows = (int64_t)p->nframes * p->nfields;
   if (!p->fstage) {
@@ -2103,6 +2105,23 @@ static shm_status persistent_ready(shm_plan* p) {
     if (st != SHM_OK) return st;
     p->gsync = g;
     p->coop_max = m * nsm;
+  }
+  return SHM_OK;
+}
+
+extern "C" shm_status shm_set_frame_staging(shm_plan* p, int64_t values) {
+  if (!p) return SHM_ERR_BAD_ARG;
+  if (values < 1) return bad(p, "frame staging needs at least one value");
+  if (values != p->fstage_n) {  // the buffers are re-made at the next readback
+    if (p->fstage) {
+      CKP(p, cudaStreamSynchronize(p->stream));
+      p->allocs.erase(std::find(p->allocs.begin(), p->allocs.end(), (void*)p->fstage));
+      cudaFree(p->fstage);
+      p->fstage = nullptr;
+    }
+    if (p->hstage) cudaFreeHost(p->hstage);
+    p->hstage = nullptr;
+    p->fstage_n = values;
   }
   return SHM_OK;
 }

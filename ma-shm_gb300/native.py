@@ -74,6 +74,7 @@ SIGNATURES = {
     "shm_forward": (C.c_int, [C.c_void_p, F64P, F64P, F64P, F64P, C.c_void_p]),
     "shm_set_guard_interval": (C.c_int, [C.c_void_p, C.c_int32]),
     "shm_set_persistent": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "shm_set_frame_staging": (C.c_int, [C.c_void_p, C.c_int64]),
     "shm_reset": (C.c_int, [C.c_void_p]),
     "shm_set_signal": (C.c_int, [C.c_void_p, F64P, C.c_void_p]),
     "shm_advance": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),

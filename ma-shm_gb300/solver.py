@@ -124,6 +124,10 @@ class Plan:
         self._check(self.lib.shm_set_persistent(self.handle, int(bool(enable)), int(spin_limit)))
         self._refresh_info()
 
+    def set_frame_staging(self, values: int):
+        """Values per staging buffer of the frame readback (default 4 M)."""
+        self._check(self.lib.shm_set_frame_staging(self.handle, int(values)))
+
     def set_guard_interval(self, steps: int):
         """Blow-up guard every ``steps`` time steps besides the frame steps
         (0: at frame steps only, as the reference)."""

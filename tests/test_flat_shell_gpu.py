@@ -469,3 +469,28 @@ def test_all_frame_fields_match_oracle(pkg, precision, path):
         sl = slice(5 * kind, 5 * kind + 5)
         assert np.abs(ref["frames"][:, sl]).max() > 0
         assert rel(got[:, sl], ref["frames"][:, sl]) <= tols[kind], kind
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_frame_readback_through_small_staging(pkg, precision):
+    """Frames reach the caller through staging buffers: with buffers smaller
+    than one frame row of a scenario (every row is cut into pieces) and
+    smaller than a few rows (runs of whole rows), across three scenarios of
+    uneven size, the returned frames are the same bits as with the default
+    buffers (the readback only moves and widens values)."""
+    scs = [pkg.workloads.random_plate(np.random.default_rng([6, s]), edge=6.25e-3, nmin=12, nmax=30)
+           for s in range(3)]
+    dt, nft = 7e-8, 120
+    for sc in scs:
+        _, sc.signal = pkg.hanning_signal(dt, nft, sc.carrier / 5, sc.carrier)
+    run = pkg.RunConfig(dt=dt, nft=nft, eta_xy=4e2, eta_z=4e3, h=3.9e-3, frm_int=20, frame_kind=3, frame_dof=0)
+    plan = pkg.Plan(scs, run, precision=precision, path=0)
+    ref = plan.forward(want_frames=True)
+    nodes = [np.asarray(sc.mesh["coords"]).shape[0] for sc in scs]
+    for values in (min(nodes) // 3, 3 * max(nodes) + 7):
+        plan.set_frame_staging(values)
+        got = plan.forward(want_frames=True)
+        for a, b in zip(got, ref):
+            assert np.abs(b["frames"]).max() > 0
+            np.testing.assert_array_equal(a["frames"], b["frames"])
+    plan.close()
