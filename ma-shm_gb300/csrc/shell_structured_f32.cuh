@@ -301,7 +301,7 @@ __device__ __forceinline__ void struct_f32_step(const F32Args& a, int kstep, uns
   const int g = lane / EW;
   const int q = lane % EW;
   float* ys = sm + SM::YS + lane * ELEM_STRIDE;
-  const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
+  const bool frame = !kAdj && a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;  // (no frames in the adjoint)
   const bool guard = guard_step(a.fs, nn);
   const int ntg = (a.ntask + G - 1) / G;
   bool bad = false, late = false;
