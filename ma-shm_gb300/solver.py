@@ -248,8 +248,9 @@ class Plan:
         for sc in self.scenarios:
             no, ns = len(sc.out_dof), len(sc.sensors)
             nnode = np.asarray(sc.mesh["coords"]).shape[0]
-            d = displ[o * self.nft:(o + no) * self.nft].reshape(no, self.nft).T.copy()
-            v = volt[s_ * self.nft:(s_ + ns) * self.nft].reshape(ns, self.nft).T.copy()
+            # [nft, n] views of the library's [n][nft] arrays (the MATLAB layout)
+            d = displ[o * self.nft:(o + no) * self.nft].reshape(no, self.nft).T
+            v = volt[s_ * self.nft:(s_ + ns) * self.nft].reshape(ns, self.nft).T
             res = dict(displ=d, voltage=v)
             if frames is not None:
                 nfr, nfl = self.info["nframes"], self.info["nfields"]
