@@ -93,3 +93,16 @@ def test_persistent_needs_an_fp32_structured_plan(pkg):
         assert ei.value.status == pkg.native.SHM_ERR_BAD_ARG
         plan.set_persistent(False)
         plan.close()
+
+
+def test_persistent_with_pressure_loading(pkg):
+    """Pressure loading (interpolated nodal frames) and frames: the persistent
+    launch reads the pressure weights of each step like the per-step launches."""
+    scs, run = pkg.workloads.plate_pressure(nft=200)
+    (ra, Ua, _), (rb, Ub, _) = run_both(pkg, scs, run, tile_elems=32, rows_per_block=2)
+    for a, b in zip(ra, rb):
+        np.testing.assert_array_equal(a["displ"], b["displ"])
+        if run.frm_int > 0:
+            np.testing.assert_array_equal(a["frames"], b["frames"])
+    assert np.abs(Ua).max() > 0
+    np.testing.assert_array_equal(Ua, Ub)
