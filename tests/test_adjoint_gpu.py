@@ -154,3 +154,25 @@ def test_adjoint_stored_segments_equal_recompute(pkg, path):
     for name in ("part", "all"):
         np.testing.assert_array_equal(got[name][1][0], got["none"][1][0])
         assert got[name][0][0] == got["none"][0][0]
+
+
+def test_adjoint_with_persistent_forward(pkg):
+    """A plan that steps persistently runs the forward pass of
+    forward_backward in the persistent kernel (the recompute and the adjoint
+    sweep keep their per-step launches): the states are the same bits, so
+    misfit and gradient equal those of the per-step plan exactly, with part of
+    the segments stored and the rest recomputed."""
+    sc, run, target = adjoint_case(pkg, seed=6)
+    got = {}
+    for persistent in (False, True):
+        plan = pkg.Plan([sc], run, precision=32, path=2)
+        if persistent:
+            plan.set_persistent(True)
+        k = 30
+        nck = -(-(run.nft - run.nn_first + 1) // k)
+        plan.set_adjoint_store((nck // 2) * k * 4 * 5 * plan.info["nnode"])
+        got[persistent] = plan.forward_backward([target], ckpt_every=k)
+        assert 0 < plan.stored_segments() < nck
+        plan.close()
+    np.testing.assert_array_equal(got[True][1][0], got[False][1][0])
+    assert got[True][0][0] == got[False][0][0]
