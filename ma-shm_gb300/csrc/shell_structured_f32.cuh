@@ -538,22 +538,18 @@ __device__ __forceinline__ void struct_f32_step(const F32Args& a, int kstep, uns
         }
         if (kSensor) vred[i * CTA_ELEMS + lane] = vp;
         if constexpr (kAdj) {
-          // column i's share of lambda' K_e^0 u_{n-1} (the row part is added
-          // in phase C), then keep_e K_e^0 lambda
+          // lambda' K_e^0 u_{n-1} over the element's nodes: here only row 0's
+          // column part (row 0 joins the carried band row, so it is scaled by
+          // keep_e now).  Rows 1-5 of the column part stay unscaled in the
+          // band (and in `edge`): phase C adds the row part there, takes the
+          // node's whole term and scales.
           if (valid) {
             const float* umc = a.um + t.node0 + (int64_t)(5 * (t.eyA + r)) * t.NX + 5 * ex + i;
 #pragma unroll
-            for (int f = 0; f < 5; ++f)
-#pragma unroll
-              for (int p = 0; p < 3; ++p) {
-                dl += Fe2[f][p].x * umc[f * a.nnode_pad + (2 * p) * t.NX];
-                dl += Fe2[f][p].y * umc[f * a.nnode_pad + (2 * p + 1) * t.NX];
-              }
+            for (int f = 0; f < 5; ++f) dl += Fe2[f][0].x * umc[f * a.nnode_pad];
           }
 #pragma unroll
-          for (int f = 0; f < 5; ++f)
-#pragma unroll
-            for (int p = 0; p < 3; ++p) Fe2[f][p] = mul2(Fe2[f][p], bc2(keep));
+          for (int f = 0; f < 5; ++f) Fe2[f][0].x *= keep;
         }
         // column part at rows m = 0..5 of column i (zeros from lanes without
         // an element, so that stale band values never survive)
@@ -619,19 +615,23 @@ __device__ __forceinline__ void struct_f32_step(const F32Args& a, int kstep, uns
         }
       }
       if constexpr (kAdj) {
-        // line j's row part of lambda' K_e^0 u_{n-1}, then keep_e K_e^0 lambda
-        if (valid) {
-          const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
-#pragma unroll
-          for (int f = 0; f < 5; ++f)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) dl += out[f][i] * umr[f * a.nnode_pad + i];
-          vred[j * CTA_ELEMS + lane] = dl;
-        }
+        // K_e^0 lambda at the element's nodes of line j: the row part plus,
+        // for j > 0, the element's own column part (unscaled in the band, in
+        // `edge` for column 5 unless this is the strip's last lane); its
+        // product with u_{n-1} is the line's share of lambda' K_e^0 u_{n-1};
+        // then keep_e K_e^0 lambda for the band
+        const float* bsrc = fb + prow_of(j) * 5 * W + 5 * q;
+        const float* umr = a.um + t.node0 + (int64_t)(5 * (t.eyA + r) + j) * t.NX + 5 * ex;
 #pragma unroll
         for (int f = 0; f < 5; ++f)
 #pragma unroll
-          for (int i = 0; i < NP; ++i) out[f][i] *= keep;
+          for (int i = 0; i < NP; ++i) {
+            float tot = out[f][i];
+            if (j > 0) tot += (i < 5 || q == EW - 1) ? bsrc[f * W + i] : edge[(j * 5 + f) * CTA_ELEMS + lane];
+            if (valid) dl += tot * umr[f * a.nnode_pad + i];
+            out[f][i] = keep * tot;
+          }
+        if (valid) vred[j * CTA_ELEMS + lane] = dl;
       }
       // band accumulation: logical row j of this element row is physical row
       // (j - r) mod 6 and already holds the column part (phase B).  Column
@@ -641,18 +641,36 @@ __device__ __forceinline__ void struct_f32_step(const F32Args& a, int kstep, uns
       const int prow = prow_of(j);
       {
         float* bdst = fb + prow * 5 * W + 5 * q;
+        if (kAdj && j > 0) {
+          // out holds keep_e x (column + row part) of the element's nodes: it
+          // replaces the band entries; column 5 is the next lane's column 0
 #pragma unroll
-        for (int f = 0; f < 5; ++f) {
-          const float from_left = __shfl_up_sync(0xffffffffu, out[f][5], 1);
-          if (q > 0) out[f][0] += from_left + edge[(j * 5 + f) * CTA_ELEMS + lane - 1];
-        }
+          for (int f = 0; f < 5; ++f) {
+            const float from_left = __shfl_up_sync(0xffffffffu, out[f][5], 1);
+            if (q > 0) out[f][0] += from_left;
+          }
 #pragma unroll
-        for (int f = 0; f < 5; ++f)
+          for (int f = 0; f < 5; ++f)
 #pragma unroll
-          for (int i = 0; i < 5; ++i) bdst[f * W + i] += out[f][i];
-        if (q == EW - 1) {
+            for (int i = 0; i < 5; ++i) bdst[f * W + i] = out[f][i];
+          if (q == EW - 1) {
 #pragma unroll
-          for (int f = 0; f < 5; ++f) bdst[f * W + 5] += out[f][5];
+            for (int f = 0; f < 5; ++f) bdst[f * W + 5] = out[f][5];
+          }
+        } else {
+#pragma unroll
+          for (int f = 0; f < 5; ++f) {
+            const float from_left = __shfl_up_sync(0xffffffffu, out[f][5], 1);
+            if (q > 0) out[f][0] += from_left + edge[(j * 5 + f) * CTA_ELEMS + lane - 1];
+          }
+#pragma unroll
+          for (int f = 0; f < 5; ++f)
+#pragma unroll
+            for (int i = 0; i < 5; ++i) bdst[f * W + i] += out[f][i];
+          if (q == EW - 1) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) bdst[f * W + 5] += out[f][5];
+          }
         }
         // band row j is now complete and written by this warp alone (the
         // column parts of all warps were stored before the third barrier),
