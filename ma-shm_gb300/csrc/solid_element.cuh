@@ -525,10 +525,25 @@ __global__ void __launch_bounds__(256) k_node_solid(SolidArgs<T> a, int kstep) {
   const T* __restrict__ cur = odd ? a.UB : a.UA;
   T* prev = odd ? a.UA : a.UB;
   T F[3] = {T(0), T(0), T(0)};
-  for (int s = a.row_ptr[g]; s < a.row_ptr[g + 1]; ++s) {
-    const int64_t slot = a.slots[s];
+  // the copies in runs of up to four: their slot numbers, then their values,
+  // are read together; the sum keeps the basket order
+  const int s0 = a.row_ptr[g], s1 = a.row_ptr[g + 1];
+  for (int s = s0; s < s1; s += 4) {
+    const int n = min(4, s1 - s);
+    int64_t sl[4];
 #pragma unroll
-    for (int f = 0; f < 3; ++f) F[f] += a.F2[f * a.plane + slot];
+    for (int k = 0; k < 4; ++k) sl[k] = k < n ? a.slots[s + k] : 0;
+    T v[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int f = 0; f < 3; ++f) v[k][f] = k < n ? a.F2[f * a.plane + sl[k]] : T(0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < n) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) F[f] += v[k][f];
+      }
   }
   const T im = a.minv[g];
   const bool frame = a.fs.frm_int > 0 && (nn % a.fs.frm_int) == 0;
