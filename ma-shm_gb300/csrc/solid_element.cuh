@@ -97,7 +97,7 @@ constexpr int S_TPE = 18;                       // threads per element
 constexpr int S_ES = 1650;                      // element stride in shared memory (values)
 static_assert(S_ES >= 15 * S_NPE && S_ES % 32 == 18, "element stride");
 template <typename T> struct SolidLines {   // (instantiated for FP32)
-  static constexpr int EPB = 16;                      // elements per CTA (106 KB)
+  static constexpr int EPB = 8;                       // elements per CTA (53 KB)
   static constexpr int THREADS = S_TPE * EPB;
   static constexpr size_t SMEM = sizeof(T) * (size_t)S_ES * EPB;
 };
