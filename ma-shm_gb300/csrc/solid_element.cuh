@@ -82,7 +82,8 @@ template <typename T> struct SolidArgs {
 // once per node.  The element stride is 18 mod 32 words: consecutive threads
 // then touch consecutive banks across an element boundary too, which the
 // per-node accesses (most of the shared-memory traffic) need.
-//   phase 0  gather u (conn) into both orders
+//   phase 0  stage the element group's u, gathered through the connectivity
+//            while the previous group was computed, in both orders
 //   phase 1  derivatives along the thread's xi, eta and zeta lines
 //   phase 2  per node: physical gradient, strains, stresses, weighted fluxes
 //   phase 3  transposed operators along the xi and eta lines (into the u
