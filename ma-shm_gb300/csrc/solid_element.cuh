@@ -23,7 +23,7 @@ namespace shm {
 
 constexpr int S_NZ = 3;
 constexpr int S_NPE = NP * NP * S_NZ;   // 108 nodes per element
-constexpr int S_EPB = 16;               // element padding (a multiple of the elements per CTA)
+constexpr int S_EPB = 48;               // element padding (a multiple of the elements per CTA)
 constexpr int S_MAT = 14;               // D11 D12 D13 D14 D22 D23 D24 D33 D34 D44 D55 D56 D66 rho
 constexpr int S_MAT_DEV = 16;
 
@@ -98,7 +98,10 @@ constexpr int S_TPE = 18;                       // threads per element
 constexpr int S_ES = 1650;                      // element stride in shared memory (values)
 static_assert(S_ES >= 15 * S_NPE && S_ES % 32 == 18, "element stride");
 template <typename T> struct SolidLines {   // (instantiated for FP32)
-  static constexpr int EPB = 8;                       // elements per CTA (53 KB)
+  // elements per CTA: 12 (79 KB, two CTAs per SM) leaves ~98 KB of L1 for the
+  // connectivity gathers and measured faster than 8 (four CTAs, ~45 KB of L1)
+  // and 16 (two CTAs, ~45 KB)
+  static constexpr int EPB = 12;
   static constexpr int THREADS = S_TPE * EPB;
   static constexpr size_t SMEM = sizeof(T) * (size_t)S_ES * EPB;
 };
