@@ -1871,6 +1871,7 @@ static shm_status frames_to_host(shm_plan* p, double* frames, cudaStream_t s) {
   int64_t host_off = 0;
   for (int sc = 0; sc < p->nscen; ++sc) {
     const int64_t n0 = p->node_off[sc], nn = p->node_off[sc + 1] - n0;
+    if (nn <= 0) continue;
     const int64_t cw = std::min(nn, kStage);                       // columns per piece
     const int64_t per = nn <= kStage ? std::max<int64_t>(1, kStage / std::max<int64_t>(nn, 1)) : 1;
     for (int64_t r0 = 0; r0 < rows; r0 += per) {
