@@ -41,3 +41,13 @@ def test_bad_arguments_fail_without_gpu_work(built_pkg):
     st = lib.shm_plan_create(0, None, None, None, None, ctypes.byref(h))
     assert st == built_pkg.native.SHM_ERR_BAD_ARG
     assert lib.shm_plan_destroy(None) == built_pkg.native.SHM_OK
+
+
+def test_plan_settings_reject_a_null_plan(built_pkg):
+    """The plan settings refuse a NULL plan before touching the device."""
+    lib = built_pkg.native.load()
+    bad = built_pkg.native.SHM_ERR_BAD_ARG
+    assert lib.shm_set_persistent(None, 1, -1) == bad
+    assert lib.shm_set_frame_staging(None, 1024) == bad
+    assert lib.shm_set_guard_interval(None, 100) == bad
+    assert lib.shm_set_adjoint_store(None, 0, None) == bad
